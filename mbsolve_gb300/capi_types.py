@@ -1,0 +1,147 @@
+"""ctypes mirrors of the structs in include/mbsolve_gb300.h.
+
+Pure data definitions: importing this module loads no native library.
+"""
+import ctypes as C
+
+MBG_OK = 0
+MBG_ERR_INVALID_ARGUMENT = 1
+MBG_ERR_CUDA = 2
+MBG_ERR_RUNTIME = 3
+
+MBG_SOURCE_HARD, MBG_SOURCE_SOFT = 0, 1
+MBG_SHAPE_TABLE, MBG_SHAPE_SECH, MBG_SHAPE_GAUSSIAN = 0, 1, 2
+(MBG_RECORD_ELECTRIC, MBG_RECORD_POLAR_DT, MBG_RECORD_MAGNETIC,
+ MBG_RECORD_DENSITY, MBG_RECORD_INVERSION) = range(5)
+MBG_RELAX_NONE, MBG_RELAX_LINDBLAD = 0, 1
+MBG_FIELD_IC_CONST, MBG_FIELD_IC_VALUES = 0, 1
+
+PD = C.POINTER(C.c_double)
+
+
+class mbg_qm(C.Structure):
+    _fields_ = [
+        ("num_levels", C.c_uint32),
+        ("carrier_density", C.c_double),
+        ("h_diag", PD),
+        ("h_off", PD),
+        ("mu_diag", PD),
+        ("mu_off", PD),
+        ("relax_kind", C.c_int32),
+        ("scattering", PD),
+        ("dephasing", PD),
+    ]
+
+
+class mbg_material(C.Structure):
+    _fields_ = [
+        ("rel_permittivity", C.c_double),
+        ("rel_permeability", C.c_double),
+        ("overlap_factor", C.c_double),
+        ("losses", C.c_double),
+        ("qm", C.POINTER(mbg_qm)),
+    ]
+
+
+class mbg_region(C.Structure):
+    _fields_ = [
+        ("material", C.c_uint32),
+        ("x_start", C.c_double),
+        ("x_end", C.c_double),
+    ]
+
+
+class mbg_device(C.Structure):
+    _fields_ = [
+        ("num_materials", C.c_uint32),
+        ("materials", C.POINTER(mbg_material)),
+        ("num_regions", C.c_uint32),
+        ("regions", C.POINTER(mbg_region)),
+    ]
+
+
+class mbg_source(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32),
+        ("shape", C.c_int32),
+        ("position", C.c_double),
+        ("ampl", C.c_double),
+        ("freq", C.c_double),
+        ("phase", C.c_double),
+        ("beta_or_tau", C.c_double),
+        ("phase_sin", C.c_double),
+        ("table", PD),
+        ("table_len", C.c_uint32),
+    ]
+
+
+class mbg_record(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32),
+        ("row", C.c_uint32),
+        ("col", C.c_uint32),
+        ("interval", C.c_double),
+        ("position", C.c_double),
+        ("is_complex", C.c_int32),
+    ]
+
+
+class mbg_scenario(C.Structure):
+    _fields_ = [
+        ("num_gridpoints", C.c_uint32),
+        ("endtime", C.c_double),
+        ("num_timesteps", C.c_uint32),
+        ("rho_diag", PD),
+        ("rho_off", PD),
+        ("rho_levels", C.c_uint32),
+        ("rho_num_off", C.c_uint32),
+        ("e_init_kind", C.c_int32),
+        ("e_init_value", C.c_double),
+        ("e_init_values", PD),
+        ("h_init_kind", C.c_int32),
+        ("h_init_value", C.c_double),
+        ("h_init_values", PD),
+        ("num_sources", C.c_uint32),
+        ("sources", C.POINTER(mbg_source)),
+        ("num_records", C.c_uint32),
+        ("records", C.POINTER(mbg_record)),
+    ]
+
+
+class mbg_grid(C.Structure):
+    _fields_ = [
+        ("num_gridpoints", C.c_uint32),
+        ("num_timesteps", C.c_uint32),
+        ("gridpoint_size", C.c_double),
+        ("timestep_size", C.c_double),
+        ("endtime", C.c_double),
+    ]
+
+
+class mbg_tuning(C.Structure):
+    _fields_ = [
+        ("cells_per_thread", C.c_uint32),
+        ("threads", C.c_uint32),
+        ("depth", C.c_uint32),
+        ("launches_per_graph", C.c_uint32),
+    ]
+
+
+def dbuf(values):
+    """A ctypes double array holding `values` (kept alive by the caller)."""
+    vals = list(values)
+    arr = (C.c_double * max(1, len(vals)))(*vals)
+    return arr
+
+
+class PodBundle:
+    """Owns every ctypes buffer a device/scenario description points into."""
+
+    def __init__(self):
+        self.keep = []
+        self.device = None
+        self.scenario = None
+
+    def hold(self, obj):
+        self.keep.append(obj)
+        return obj

@@ -1,0 +1,869 @@
+// Time-step kernels of the Maxwell-Bloch loop.
+//
+// One kernel launch advances every tile of every run by up to `nsub` time
+// steps (temporal blocking). A CTA owns NT*C consecutive grid points of one
+// run, C per thread in registers, and keeps them on chip for all sub-steps:
+//   state in  : [out_start - halo, out_start + out_len + halo)
+//   state out : [out_start, out_start + out_len)
+// Each sub-step reproduces one iteration of solver_cpu_fdtd::run
+// (solver-cpu/include/mbsolve/solver-cpu/solver_cpu_fdtd.tpp:223-325):
+//   E[i] = a E[i] + b (-Gamma P[i] + (H[i+1] - H[i]) / dx)      (:238-243)
+//   hard/soft sources on E                                       (:247-255)
+//   H[i] += c (E[i] - E[i-1]), i >= 1; H[0] = H[N] = 0          (:263-275)
+//   density update and P[i] = dP/dt at every point              (:279-285)
+//   recording                                                    (:288-325)
+// Neighbour values cross thread boundaries by warp shuffles and cross warp
+// boundaries through shared memory (two barriers per step). Garbage from
+// the tile edges moves one point per step, so after `nsub <= halo` steps
+// the output range is exact. Points outside the run carry zero
+// coefficients and zero state; the reference's index rules (no H update at
+// i = 0, H[N] = 0) give them no influence on the run.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "precompute.cuh"
+
+namespace mbg {
+
+template<typename T>
+struct kparams {
+    const T* Ein;
+    const T* Hin;
+    const T* Pin;
+    const T* Din;  // density planes, `plane` apart
+    T* Eout;
+    T* Hout;
+    T* Pout;
+    T* Dout;
+    uint64_t plane;
+    const int32_t* mat;  // global material index per point (-1: none)
+    const T* mc;         // material constant blocks
+    uint32_t mstride;
+    uint32_t mstage;     // leading entries of a block staged in shared memory
+    const tile_desc* tiles;
+    const run_desc* runs;
+    const src_desc* srcs;
+    const T* stab;       // source value tables
+    const rec_desc* recs;
+    T* scratch;
+    const unsigned long long* step_base;  // device step counter
+    uint32_t launch_idx;  // step0 = *step_base + launch_idx * depth
+    uint32_t depth;
+    uint32_t nsub;        // sub-steps of this launch (<= depth)
+    uint32_t halo;
+    int record;           // 0 while autotuning
+    uint32_t* status;
+};
+
+// ------------------------------------------------------------ helpers
+
+// sin(x) and 1 - cos(x). For |x| < 1/4 by their Taylor series (enough
+// terms for the type's precision: truncation below 1e-16 relative in
+// float, 1e-30 in double); beyond that by the library sincos.
+template<typename T>
+__device__ __forceinline__ void rot_coeffs(T x, T& s, T& s2);
+
+template<>
+__device__ __forceinline__ void rot_coeffs<float>(float x, float& s, float& s2)
+{
+    if (fabsf(x) < 0.25f) {
+        float x2 = x * x;
+        // sin x = x (1 - x^2/(2*3) (1 - x^2/(4*5) (1 - x^2/(6*7) (1 - x^2/(8*9)))))
+        float t = 1.0f - x2 * (1.0f / 72.0f);
+        t = 1.0f - x2 * (1.0f / 42.0f) * t;
+        t = 1.0f - x2 * (1.0f / 20.0f) * t;
+        t = 1.0f - x2 * (1.0f / 6.0f) * t;
+        s = x * t;
+        // 1 - cos x = x^2/2 (1 - x^2/(3*4) (1 - x^2/(5*6) (1 - x^2/(7*8) (1 - x^2/(9*10)))))
+        float u = 1.0f - x2 * (1.0f / 90.0f);
+        u = 1.0f - x2 * (1.0f / 56.0f) * u;
+        u = 1.0f - x2 * (1.0f / 30.0f) * u;
+        u = 1.0f - x2 * (1.0f / 12.0f) * u;
+        s2 = 0.5f * x2 * u;
+    } else {
+        float c;
+        sincosf(x, &s, &c);
+        s2 = 1.0f - c;
+    }
+}
+
+template<>
+__device__ __forceinline__ void rot_coeffs<double>(double x, double& s, double& s2)
+{
+    if (fabs(x) < 0.25) {
+        double x2 = x * x;
+        double t = 1.0, u = 1.0;
+#pragma unroll
+        for (int k = 10; k >= 1; k--) {
+            t = 1.0 - x2 / ((2.0 * k) * (2.0 * k + 1.0)) * t;
+            u = 1.0 - x2 / ((2.0 * k + 1.0) * (2.0 * k + 2.0)) * u;
+        }
+        s = x * t;
+        s2 = 0.5 * x2 * u;
+    } else {
+        double c;
+        sincos(x, &s, &c);
+        s2 = 1.0 - c;
+    }
+}
+
+template<typename T, int C>
+__device__ __forceinline__ void load_cells(T (&r)[C], const T* __restrict__ src, int64_t g0)
+{
+    if constexpr (sizeof(T) == 4 && (C % 4) == 0) {
+        const float4* s4 = reinterpret_cast<const float4*>(src + g0);
+#pragma unroll
+        for (int q = 0; q < C / 4; q++) {
+            float4 v = __ldcs(s4 + q);
+            r[4 * q + 0] = v.x;
+            r[4 * q + 1] = v.y;
+            r[4 * q + 2] = v.z;
+            r[4 * q + 3] = v.w;
+        }
+    } else if constexpr (sizeof(T) == 8 && (C % 2) == 0) {
+        const double2* s2 = reinterpret_cast<const double2*>(src + g0);
+#pragma unroll
+        for (int q = 0; q < C / 2; q++) {
+            double2 v = __ldcs(s2 + q);
+            r[2 * q + 0] = v.x;
+            r[2 * q + 1] = v.y;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < C; j++) r[j] = __ldcs(src + g0 + j);
+    }
+}
+
+template<typename T, int C>
+__device__ __forceinline__ void store_cells(
+    const T (&r)[C],
+    T* __restrict__ dst,
+    int64_t g0,
+    int64_t l0,
+    int64_t lo,
+    int64_t hi)
+{
+    if (l0 >= lo && l0 + C <= hi) {
+        if constexpr (sizeof(T) == 4 && (C % 4) == 0) {
+            float4* d4 = reinterpret_cast<float4*>(dst + g0);
+#pragma unroll
+            for (int q = 0; q < C / 4; q++)
+                __stcs(d4 + q, make_float4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]));
+            return;
+        } else if constexpr (sizeof(T) == 8 && (C % 2) == 0) {
+            double2* d2 = reinterpret_cast<double2*>(dst + g0);
+#pragma unroll
+            for (int q = 0; q < C / 2; q++) __stcs(d2 + q, make_double2(r[2 * q], r[2 * q + 1]));
+            return;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < C; j++)
+        if (l0 + j >= lo && l0 + j < hi) dst[g0 + j] = r[j];
+}
+
+// Coefficients of the coherence-vector update, read through a pointer
+// (shared memory for uniform tiles, global memory otherwise).
+template<typename T, int V>
+struct cvr_coef {
+    static constexpr int KP = V / 2;
+    static constexpr int oBd = 8;
+    static constexpr int oc = 8 + V * V;
+    static constexpr int og = oc + V;
+    static constexpr int oth = og + V;
+    const T* base;
+    __device__ __forceinline__ T Bd(int i, int j) const { return base[oBd + i * V + j]; }
+    __device__ __forceinline__ T c(int i) const { return base[oc + i]; }
+    __device__ __forceinline__ T g(int i) const { return base[og + i]; }
+    __device__ __forceinline__ T th(int k) const { return base[oth + k]; }
+    __device__ __forceinline__ T p0() const { return base[5]; }
+};
+
+// Coherence-vector update in the plane basis (see precompute.cuh):
+// w = z + Bd z - c; rotate each plane by theta_k dt e; z = (w + c) + Bd (w + c);
+// P = p0 + g . z.
+template<typename T, int V, class CF>
+__device__ __forceinline__ void cvr_update(T (&z)[V], T e, T& pout, const CF& cf)
+{
+    T w[V];
+#pragma unroll
+    for (int i = 0; i < V; i++) {
+        T s = z[i] - cf.c(i);
+#pragma unroll
+        for (int j = 0; j < V; j++) s = fma(cf.Bd(i, j), z[j], s);
+        w[i] = s;
+    }
+#pragma unroll
+    for (int k = 0; k < V / 2; k++) {
+        T sn, s2;
+        rot_coeffs<T>(cf.th(k) * e, sn, s2);
+        T a = w[2 * k], b = w[2 * k + 1];
+        w[2 * k] = a - fma(s2, a, sn * b);
+        w[2 * k + 1] = b + fma(sn, a, -s2 * b);
+    }
+#pragma unroll
+    for (int i = 0; i < V; i++) w[i] += cf.c(i);
+    T pp = cf.p0();
+#pragma unroll
+    for (int i = 0; i < V; i++) {
+        T s = w[i];
+#pragma unroll
+        for (int j = 0; j < V; j++) s = fma(cf.Bd(i, j), w[j], s);
+        z[i] = s;
+        pp = fma(cf.g(i), s, pp);
+    }
+    pout = pp;
+}
+
+// Value of a record at one point (solver_cpu_fdtd.tpp:301-325).
+template<typename T, int V>
+__device__ __forceinline__ T cvr_record_value(
+    const rec_desc& rc,
+    T e,
+    T h,
+    T pt,
+    const T (&z)[V > 0 ? V : 1],
+    const T* mcb,
+    int N)
+{
+    switch (rc.type) {
+    case 0:
+        return e;
+    case 1:
+        return pt;
+    case 2:
+        return h;
+    case 4: {  // inversion d[N(N-1)]
+        if (V == 0) return T(0);
+        pre::cvr_layout L = pre::make_cvr_layout(N);
+        T s = mcb[L.inv_c];
+#pragma unroll
+        for (int k = 0; k < (V > 0 ? V : 1); k++) s += mcb[L.inv + k] * z[k];
+        return s;
+    }
+    case 3: {
+        if (V == 0) return T(0);
+        if (rc.row_idx != rc.col_idx) return T(0);  // coherences: left zero
+        pre::cvr_layout L = pre::make_cvr_layout(N);
+        int m = (int) rc.row_idx;
+        // out-of-range level: what cvr.hpp:289-336 returns for it
+        if (m >= N) {
+            if (N == 2)
+                m = 1;
+            else
+                return (N == 3) ? T(0) : T(1.0 / N);
+        }
+        T s = mcb[L.pop_c + m];
+#pragma unroll
+        for (int k = 0; k < (V > 0 ? V : 1); k++) s += mcb[L.pop + m * (V > 0 ? V : 1) + k] * z[k];
+        return s;
+    }
+    }
+    return T(0);
+}
+
+template<typename T>
+__device__ __forceinline__ void store_record(
+    const kparams<T>& p,
+    const rec_desc& rc,
+    uint64_t n,
+    int64_t l,
+    T v)
+{
+    uint64_t row = (uint64_t) floor(rc.ratio * (double) n);
+    if (row >= rc.rows) return;
+    p.scratch[rc.offset + row * rc.cols + (uint64_t) (l - rc.pos)] = v;
+    if (!isfinite(v)) atomicOr(p.status, STATUS_NONFINITE);
+}
+
+// --------------------------------------------------- CVR / Maxwell kernel
+//
+// V = N^2 - 1 density reals per point (V = 0: Maxwell only, the noop
+// algorithm of algo_lindblad_noop.hpp).
+template<typename T, int V, int C, int NT>
+__global__ void __launch_bounds__(NT) cvr_step_kernel(const kparams<T> p)
+{
+    constexpr int NW = NT / 32;
+    constexpr int VV = V > 0 ? V : 1;
+    constexpr int NLEV = V == 3 ? 2 : V == 8 ? 3 : V == 15 ? 4 : V == 24 ? 5 : V == 35 ? 6 : 0;
+    __shared__ T sh_h[NW];
+    __shared__ T sh_e[NW];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sh_coef = reinterpret_cast<T*>(smem_raw);
+
+    const tile_desc td = p.tiles[blockIdx.x];
+    const run_desc rd = p.runs[td.run];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int64_t l0 = (int64_t) td.out_start - (int64_t) p.halo + (int64_t) threadIdx.x * C;
+    const int64_t g0 = (int64_t) rd.offset + l0;
+    const int64_t nx = rd.n_x;
+    const uint64_t step0 = *p.step_base + (uint64_t) p.launch_idx * p.depth;
+    int nsteps = 0;
+    if (step0 < rd.n_t) nsteps = (int) min((uint64_t) p.nsub, (uint64_t) rd.n_t - step0);
+
+    T E[C], H[C], P[C];
+    T Z[C][VV];
+    int32_t M[C];
+    load_cells<T, C>(E, p.Ein, g0);
+    load_cells<T, C>(H, p.Hin, g0);
+    load_cells<T, C>(P, p.Pin, g0);
+    if constexpr (V > 0) {
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            T tmp[C];
+            load_cells<T, C>(tmp, p.Din + (uint64_t) v * p.plane, g0);
+#pragma unroll
+            for (int j = 0; j < C; j++) Z[j][v] = tmp[j];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < C; j++) {
+        const int64_t l = l0 + j;
+        const bool valid = (l >= 0) && (l < nx);
+        M[j] = valid ? __ldg(p.mat + g0 + j) : -1;
+        if (!valid) {
+            E[j] = H[j] = P[j] = T(0);
+#pragma unroll
+            for (int v = 0; v < VV; v++) Z[j][v] = T(0);
+        }
+    }
+    const bool uniform = td.uniform_mat >= 0;
+    if (uniform) {
+        const T* src = p.mc + (uint64_t) td.uniform_mat * p.mstride;
+        for (int i = threadIdx.x; i < (int) p.mstage; i += NT) sh_coef[i] = src[i];
+    }
+    __syncthreads();
+    const T dxi = (T) rd.dx_inv;
+
+    for (int m = 0; m < nsteps; m++) {
+        const uint64_t n = step0 + (uint64_t) m;
+        // ---- E update: needs H of the right neighbour
+        if (lane == 0) sh_h[warp] = H[0];
+        __syncthreads();
+        T hr = __shfl_down_sync(0xffffffffu, H[0], 1);
+        if (lane == 31) hr = (warp + 1 < NW) ? sh_h[warp + 1] : T(0);
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            const T hn = (j + 1 < C) ? H[j + 1] : hr;
+            T a, b, gam;
+            if (uniform) {
+                a = sh_coef[0];
+                b = sh_coef[1];
+                gam = sh_coef[3];
+            } else if (M[j] >= 0) {
+                const T* cb = p.mc + (uint64_t) M[j] * p.mstride;
+                a = cb[0];
+                b = cb[1];
+                gam = cb[3];
+            } else {
+                a = b = gam = T(0);
+            }
+            const bool valid = M[j] >= 0;
+            T en = a * E[j] + b * (-gam * P[j] + (hn - H[j]) * dxi);
+            E[j] = valid ? en : T(0);
+        }
+        // ---- sources (after E, before H)
+        for (uint32_t s = rd.src_begin; s < rd.src_end; s++) {
+            const src_desc sd = p.srcs[s];
+            const int64_t jj = (int64_t) sd.x_idx - l0;
+            if (jj >= 0 && jj < C) {
+                const T val = p.stab[sd.table_offset + n];
+#pragma unroll
+                for (int j = 0; j < C; j++)
+                    if (j == jj && M[j] >= 0) E[j] = (sd.type == 0) ? val : E[j] + val;
+            }
+        }
+        // ---- H update: needs E of the left neighbour
+        if (lane == 31) sh_e[warp] = E[C - 1];
+        __syncthreads();
+        T el = __shfl_up_sync(0xffffffffu, E[C - 1], 1);
+        if (lane == 0) el = (warp > 0) ? sh_e[warp - 1] : T(0);
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            const int64_t l = l0 + j;
+            const T ep = (j > 0) ? E[j - 1] : el;
+            if (l >= 1 && l < nx) {
+                T cH = uniform ? sh_coef[2] : p.mc[(uint64_t) M[j] * p.mstride + 2];
+                H[j] += cH * (E[j] - ep);
+            } else if (l == 0) {
+                H[j] = T(0);
+            }
+        }
+        // ---- density update and polarisation current
+        if constexpr (V > 0) {
+            if (uniform) {
+                if (sh_coef[4] != T(0)) {
+                    cvr_coef<T, V> cf{ sh_coef };
+#pragma unroll
+                    for (int j = 0; j < C; j++)
+                        if (M[j] >= 0) cvr_update<T, V>(Z[j], E[j], P[j], cf);
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < C; j++) {
+                    if (M[j] < 0) continue;
+                    const T* cb = p.mc + (uint64_t) M[j] * p.mstride;
+                    if (cb[4] == T(0)) continue;
+                    cvr_coef<T, V> cf{ cb };
+                    cvr_update<T, V>(Z[j], E[j], P[j], cf);
+                }
+            }
+        }
+        // ---- recording
+        if (p.record) {
+            for (uint32_t r = rd.rec_begin; r < rd.rec_end; r++) {
+                const rec_desc rc = p.recs[r];
+                if (!hasto_record(rc.ratio, n)) continue;
+                const int64_t lo = max((int64_t) rc.pos, (int64_t) td.out_start);
+                const int64_t hi = min((int64_t) rc.pos + rc.cols,
+                                       (int64_t) td.out_start + td.out_len);
+                if (l0 + C <= lo || l0 >= hi) continue;
+#pragma unroll
+                for (int j = 0; j < C; j++) {
+                    const int64_t l = l0 + j;
+                    if (l < lo || l >= hi) continue;
+                    const T* cb = p.mc + (uint64_t) (M[j] >= 0 ? M[j] : 0) * p.mstride;
+                    T v = cvr_record_value<T, V>(rc, E[j], H[j], P[j], Z[j], cb, NLEV);
+                    store_record<T>(p, rc, n, l, v);
+                }
+            }
+        }
+    }
+
+    // ---- write back the output range
+    const int64_t lo = td.out_start, hi = (int64_t) td.out_start + td.out_len;
+    store_cells<T, C>(E, p.Eout, g0, l0, lo, hi);
+    store_cells<T, C>(H, p.Hout, g0, l0, lo, hi);
+    store_cells<T, C>(P, p.Pout, g0, l0, lo, hi);
+    if constexpr (V > 0) {
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            T tmp[C];
+#pragma unroll
+            for (int j = 0; j < C; j++) tmp[j] = Z[j][v];
+            store_cells<T, C>(tmp, p.Dout + (uint64_t) v * p.plane, g0, l0, lo, hi);
+        }
+    }
+}
+
+// ---------------------------------------------------- Cayley kernel
+//
+// Density matrix per point packed as N real populations followed by the
+// upper off-diagonal triangle (column-major) as (re, im) pairs. One step of
+// lindblad_reg_cayley::update (algo_lindblad_reg_cayley.hpp:228-257):
+//   rho1 = D(rho); rho2 = U2 rho1 U2^H; rho = D(rho2);
+//   P = n Re tr((-i/hbar [H0, rho] + D'(rho)) mu)
+// with U2 = (I - m/2)^-1 (I + m/2), m = -i dt/hbar (H0 - e mu). Writing
+// K = kappa (H0 - e mu), kappa = dt/(2 hbar): U2 = I + X with
+// X = -2i (I + iK)^-1 K, so rho2 = rho1 + X rho1 + (X rho1)^H + X rho1 X^H,
+// every term a small correction (accurate in FP32). D adds (D1 - I) and
+// (D2 - 1) corrections.
+
+struct cpx_f {
+    float re, im;
+};
+struct cpx_d {
+    double re, im;
+};
+template<typename T>
+struct cpx_t;
+template<>
+struct cpx_t<float> {
+    typedef cpx_f type;
+};
+template<>
+struct cpx_t<double> {
+    typedef cpx_d type;
+};
+
+template<typename T, int N>
+__device__ __forceinline__ void cayley_update(T (&rho)[N * N], T e, T& pout, const T* cf)
+{
+    typedef typename cpx_t<T>::type cx;
+    constexpr int P = N * (N - 1) / 2;
+    const pre::cay_layout L = pre::make_cay_layout(N);
+    // full K (Hermitian), A = I + i K
+    cx K[N][N], A[N][N], Y[N][N];
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        K[i][i].re = cf[L.kH0 + i] - e * cf[L.kMu + i];
+        K[i][i].im = T(0);
+    }
+#pragma unroll
+    for (int k = 1; k < N; k++)
+#pragma unroll
+        for (int j = 0; j < k; j++) {
+            const int q = k * (k - 1) / 2 + j;
+            T re = cf[L.kH0 + N + 2 * q] - e * cf[L.kMu + N + 2 * q];
+            T im = cf[L.kH0 + N + 2 * q + 1] - e * cf[L.kMu + N + 2 * q + 1];
+            K[j][k].re = re;
+            K[j][k].im = im;
+            K[k][j].re = re;
+            K[k][j].im = -im;
+        }
+#pragma unroll
+    for (int i = 0; i < N; i++)
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            // i K = (-K.im, K.re)
+            A[i][j].re = -K[i][j].im + (i == j ? T(1) : T(0));
+            A[i][j].im = K[i][j].re;
+            Y[i][j] = K[i][j];
+        }
+    // solve A Y = K by LU without pivoting (A + A^H = 2I > 0)
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        // inverse of the pivot
+        T den = A[k][k].re * A[k][k].re + A[k][k].im * A[k][k].im;
+        cx inv;
+        inv.re = A[k][k].re / den;
+        inv.im = -A[k][k].im / den;
+#pragma unroll
+        for (int i = k + 1; i < N; i++) {
+            cx f;
+            f.re = A[i][k].re * inv.re - A[i][k].im * inv.im;
+            f.im = A[i][k].re * inv.im + A[i][k].im * inv.re;
+#pragma unroll
+            for (int j = k + 1; j < N; j++) {
+                A[i][j].re -= f.re * A[k][j].re - f.im * A[k][j].im;
+                A[i][j].im -= f.re * A[k][j].im + f.im * A[k][j].re;
+            }
+#pragma unroll
+            for (int j = 0; j < N; j++) {
+                Y[i][j].re -= f.re * Y[k][j].re - f.im * Y[k][j].im;
+                Y[i][j].im -= f.re * Y[k][j].im + f.im * Y[k][j].re;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = N - 1; k >= 0; k--) {
+        T den = A[k][k].re * A[k][k].re + A[k][k].im * A[k][k].im;
+        cx inv;
+        inv.re = A[k][k].re / den;
+        inv.im = -A[k][k].im / den;
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            cx s = Y[k][j];
+#pragma unroll
+            for (int i = k + 1; i < N; i++) {
+                s.re -= A[k][i].re * Y[i][j].re - A[k][i].im * Y[i][j].im;
+                s.im -= A[k][i].re * Y[i][j].im + A[k][i].im * Y[i][j].re;
+            }
+            Y[k][j].re = s.re * inv.re - s.im * inv.im;
+            Y[k][j].im = s.re * inv.im + s.im * inv.re;
+        }
+    }
+    // X = -2i Y  -> (2 Y.im, -2 Y.re); reuse K for X
+#pragma unroll
+    for (int i = 0; i < N; i++)
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            K[i][j].re = T(2) * Y[i][j].im;
+            K[i][j].im = T(-2) * Y[i][j].re;
+        }
+    // rho1 = D(rho): full Hermitian R in A
+    auto dissipate = [&](const T (&in)[N * N], cx (&R)[N][N]) {
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            T s = in[i];
+#pragma unroll
+            for (int j = 0; j < N; j++) s = fma(cf[L.dD1 + i * N + j], in[j], s);
+            R[i][i].re = s;
+            R[i][i].im = T(0);
+        }
+#pragma unroll
+        for (int k = 1; k < N; k++)
+#pragma unroll
+            for (int j = 0; j < k; j++) {
+                const int q = k * (k - 1) / 2 + j;
+                const T dd = cf[L.dD2 + q];
+                T re = in[N + 2 * q], im = in[N + 2 * q + 1];
+                re = fma(dd, re, re);
+                im = fma(dd, im, im);
+                R[j][k].re = re;
+                R[j][k].im = im;
+                R[k][j].re = re;
+                R[k][j].im = -im;
+            }
+    };
+    dissipate(rho, A);
+    // G = X rho1 (in Y)
+#pragma unroll
+    for (int i = 0; i < N; i++)
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            cx s;
+            s.re = T(0);
+            s.im = T(0);
+#pragma unroll
+            for (int l = 0; l < N; l++) {
+                s.re += K[i][l].re * A[l][j].re - K[i][l].im * A[l][j].im;
+                s.im += K[i][l].re * A[l][j].im + K[i][l].im * A[l][j].re;
+            }
+            Y[i][j] = s;
+        }
+    // rho2 (packed) = rho1 + G + G^H + G X^H
+    T r2[N * N];
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        T s = A[i][i].re + T(2) * Y[i][i].re;
+#pragma unroll
+        for (int l = 0; l < N; l++) s += Y[i][l].re * K[i][l].re + Y[i][l].im * K[i][l].im;
+        r2[i] = s;
+    }
+#pragma unroll
+    for (int k = 1; k < N; k++)
+#pragma unroll
+        for (int j = 0; j < k; j++) {
+            const int q = k * (k - 1) / 2 + j;
+            T re = A[j][k].re + Y[j][k].re + Y[k][j].re;
+            T im = A[j][k].im + Y[j][k].im - Y[k][j].im;
+#pragma unroll
+            for (int l = 0; l < N; l++) {
+                // G_jl conj(X_kl)
+                re += Y[j][l].re * K[k][l].re + Y[j][l].im * K[k][l].im;
+                im += Y[j][l].im * K[k][l].re - Y[j][l].re * K[k][l].im;
+            }
+            r2[N + 2 * q] = re;
+            r2[N + 2 * q + 1] = im;
+        }
+    // rho = D(rho2), full matrix in A, packed into rho
+    dissipate(r2, A);
+#pragma unroll
+    for (int i = 0; i < N; i++) rho[i] = A[i][i].re;
+#pragma unroll
+    for (int k = 1; k < N; k++)
+#pragma unroll
+        for (int j = 0; j < k; j++) {
+            const int q = k * (k - 1) / 2 + j;
+            rho[N + 2 * q] = A[j][k].re;
+            rho[N + 2 * q + 1] = A[j][k].im;
+        }
+    // P = Re tr(rhs Mn), rhs = -i [W0, rho] + D'(rho)
+    cx W[N][N], Mn[N][N];
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        W[i][i].re = cf[L.W0 + i];
+        W[i][i].im = T(0);
+        Mn[i][i].re = cf[L.Mn + i];
+        Mn[i][i].im = T(0);
+    }
+#pragma unroll
+    for (int k = 1; k < N; k++)
+#pragma unroll
+        for (int j = 0; j < k; j++) {
+            const int q = k * (k - 1) / 2 + j;
+            W[j][k].re = cf[L.W0 + N + 2 * q];
+            W[j][k].im = cf[L.W0 + N + 2 * q + 1];
+            W[k][j].re = W[j][k].re;
+            W[k][j].im = -W[j][k].im;
+            Mn[j][k].re = cf[L.Mn + N + 2 * q];
+            Mn[j][k].im = cf[L.Mn + N + 2 * q + 1];
+            Mn[k][j].re = Mn[j][k].re;
+            Mn[k][j].im = -Mn[j][k].im;
+        }
+    T acc = T(0);
+#pragma unroll
+    for (int j = 0; j < N; j++)
+#pragma unroll
+        for (int k = 0; k < N; k++) {
+            // comm_jk = sum_l W_jl rho_lk - rho_jl W_lk
+            cx cm;
+            cm.re = T(0);
+            cm.im = T(0);
+#pragma unroll
+            for (int l = 0; l < N; l++) {
+                cm.re += W[j][l].re * A[l][k].re - W[j][l].im * A[l][k].im -
+                    (A[j][l].re * W[l][k].re - A[j][l].im * W[l][k].im);
+                cm.im += W[j][l].re * A[l][k].im + W[j][l].im * A[l][k].re -
+                    (A[j][l].re * W[l][k].im + A[j][l].im * W[l][k].re);
+            }
+            // rhs_jk = -i comm_jk + D'
+            cx r;
+            r.re = cm.im;
+            r.im = -cm.re;
+            if (j == k) {
+                T s = T(0);
+#pragma unroll
+                for (int l = 0; l < N; l++) s += cf[L.d1 + j * N + l] * A[l][l].re;
+                r.re += s;
+            } else {
+                const int q = (j < k) ? k * (k - 1) / 2 + j : j * (j - 1) / 2 + k;
+                const T d2 = cf[L.d2 + q];
+                r.re += d2 * A[j][k].re;
+                r.im += d2 * A[j][k].im;
+            }
+            // Re(rhs_jk Mn_kj)
+            acc += r.re * Mn[k][j].re - r.im * Mn[k][j].im;
+        }
+    pout = acc;
+}
+
+template<typename T, int N, int C, int NT>
+__global__ void __launch_bounds__(NT) cayley_step_kernel(const kparams<T> p)
+{
+    constexpr int NW = NT / 32;
+    constexpr int D = N * N;
+    __shared__ T sh_h[NW];
+    __shared__ T sh_e[NW];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sh_coef = reinterpret_cast<T*>(smem_raw);
+
+    const tile_desc td = p.tiles[blockIdx.x];
+    const run_desc rd = p.runs[td.run];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int64_t l0 = (int64_t) td.out_start - (int64_t) p.halo + (int64_t) threadIdx.x * C;
+    const int64_t g0 = (int64_t) rd.offset + l0;
+    const int64_t nx = rd.n_x;
+    const uint64_t step0 = *p.step_base + (uint64_t) p.launch_idx * p.depth;
+    int nsteps = 0;
+    if (step0 < rd.n_t) nsteps = (int) min((uint64_t) p.nsub, (uint64_t) rd.n_t - step0);
+
+    T E[C], H[C], Pc[C];
+    T R[C][D];
+    int32_t M[C];
+    load_cells<T, C>(E, p.Ein, g0);
+    load_cells<T, C>(H, p.Hin, g0);
+    load_cells<T, C>(Pc, p.Pin, g0);
+#pragma unroll
+    for (int v = 0; v < D; v++) {
+        T tmp[C];
+        load_cells<T, C>(tmp, p.Din + (uint64_t) v * p.plane, g0);
+#pragma unroll
+        for (int j = 0; j < C; j++) R[j][v] = tmp[j];
+    }
+#pragma unroll
+    for (int j = 0; j < C; j++) {
+        const int64_t l = l0 + j;
+        const bool valid = (l >= 0) && (l < nx);
+        M[j] = valid ? __ldg(p.mat + g0 + j) : -1;
+        if (!valid) {
+            E[j] = H[j] = Pc[j] = T(0);
+#pragma unroll
+            for (int v = 0; v < D; v++) R[j][v] = T(0);
+        }
+    }
+    const bool uniform = td.uniform_mat >= 0;
+    if (uniform) {
+        const T* src = p.mc + (uint64_t) td.uniform_mat * p.mstride;
+        for (int i = threadIdx.x; i < (int) p.mstage; i += NT) sh_coef[i] = src[i];
+    }
+    __syncthreads();
+    const T dxi = (T) rd.dx_inv;
+    const pre::cay_layout L = pre::make_cay_layout(N);
+
+    for (int m = 0; m < nsteps; m++) {
+        const uint64_t n = step0 + (uint64_t) m;
+        if (lane == 0) sh_h[warp] = H[0];
+        __syncthreads();
+        T hr = __shfl_down_sync(0xffffffffu, H[0], 1);
+        if (lane == 31) hr = (warp + 1 < NW) ? sh_h[warp + 1] : T(0);
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            const T hn = (j + 1 < C) ? H[j + 1] : hr;
+            const T* cb = uniform ? sh_coef : p.mc + (uint64_t) (M[j] >= 0 ? M[j] : 0) * p.mstride;
+            const bool valid = M[j] >= 0;
+            T en = cb[0] * E[j] + cb[1] * (-cb[3] * Pc[j] + (hn - H[j]) * dxi);
+            E[j] = valid ? en : T(0);
+        }
+        for (uint32_t s = rd.src_begin; s < rd.src_end; s++) {
+            const src_desc sd = p.srcs[s];
+            const int64_t jj = (int64_t) sd.x_idx - l0;
+            if (jj >= 0 && jj < C) {
+                const T val = p.stab[sd.table_offset + n];
+#pragma unroll
+                for (int j = 0; j < C; j++)
+                    if (j == jj && M[j] >= 0) E[j] = (sd.type == 0) ? val : E[j] + val;
+            }
+        }
+        if (lane == 31) sh_e[warp] = E[C - 1];
+        __syncthreads();
+        T el = __shfl_up_sync(0xffffffffu, E[C - 1], 1);
+        if (lane == 0) el = (warp > 0) ? sh_e[warp - 1] : T(0);
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            const int64_t l = l0 + j;
+            const T ep = (j > 0) ? E[j - 1] : el;
+            if (l >= 1 && l < nx) {
+                const T* cb = uniform ? sh_coef : p.mc + (uint64_t) M[j] * p.mstride;
+                H[j] += cb[2] * (E[j] - ep);
+            } else if (l == 0) {
+                H[j] = T(0);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            if (M[j] < 0) continue;
+            const T* cb = uniform ? sh_coef : p.mc + (uint64_t) M[j] * p.mstride;
+            if (cb[4] == T(0)) continue;  // no qm: density stays zero
+            cayley_update<T, N>(R[j], E[j], Pc[j], cb);
+        }
+        if (p.record) {
+            for (uint32_t r = rd.rec_begin; r < rd.rec_end; r++) {
+                const rec_desc rc = p.recs[r];
+                if (!hasto_record(rc.ratio, n)) continue;
+                const int64_t lo = max((int64_t) rc.pos, (int64_t) td.out_start);
+                const int64_t hi = min((int64_t) rc.pos + rc.cols,
+                                       (int64_t) td.out_start + td.out_len);
+                if (l0 + C <= lo || l0 >= hi) continue;
+#pragma unroll
+                for (int j = 0; j < C; j++) {
+                    const int64_t l = l0 + j;
+                    if (l < lo || l >= hi) continue;
+                    T v = T(0);
+                    switch (rc.type) {
+                    case 0: v = E[j]; break;
+                    case 1: v = Pc[j]; break;
+                    case 2: v = H[j]; break;
+                    case 4: v = R[j][1] - R[j][0]; break;
+                    case 3:
+                        if (rc.row_idx == rc.col_idx && rc.row_idx < (uint32_t) N)
+                            v = R[j][rc.row_idx];
+                        break;
+                    }
+                    store_record<T>(p, rc, n, l, v);
+                }
+            }
+        }
+    }
+    // FP32: renormalise the trace to that of the initial density matrix, in
+    // FP64, once per launch (the exact propagators preserve the trace: the
+    // scattering matrix has zero column sums and U2 is unitary; this removes
+    // FP32 round-off drift)
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            if (M[j] < 0 || nsteps == 0) continue;
+            const T* cb = uniform ? sh_coef : p.mc + (uint64_t) M[j] * p.mstride;
+            if (cb[4] == T(0)) continue;
+            double tr = 0.0, target = 0.0;
+#pragma unroll
+            for (int i = 0; i < N; i++) {
+                tr += (double) R[j][i];
+                target += (double) cb[L.rho0 + i];
+            }
+            if (tr != 0.0 && fabs(tr / target - 1.0) < 1e-3) {
+                const float s = (float) (target / tr);
+#pragma unroll
+                for (int v = 0; v < D; v++) R[j][v] *= s;
+            }
+        }
+    }
+    const int64_t lo = td.out_start, hi = (int64_t) td.out_start + td.out_len;
+    store_cells<T, C>(E, p.Eout, g0, l0, lo, hi);
+    store_cells<T, C>(H, p.Hout, g0, l0, lo, hi);
+    store_cells<T, C>(Pc, p.Pout, g0, l0, lo, hi);
+#pragma unroll
+    for (int v = 0; v < D; v++) {
+        T tmp[C];
+#pragma unroll
+        for (int j = 0; j < C; j++) tmp[j] = R[j][v];
+        store_cells<T, C>(tmp, p.Dout + (uint64_t) v * p.plane, g0, l0, lo, hi);
+    }
+}
+
+}  // namespace mbg

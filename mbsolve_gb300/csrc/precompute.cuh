@@ -1,0 +1,886 @@
+// FP64 precompute of the per-material constants the time-step kernels use.
+//
+// One code path for host and device (__host__ __device__): the solvers run
+// it on the GPU, one thread per material; tests without a GPU run the host
+// instantiation through mbg_material_constants().
+//
+// Coherence-vector / Rodrigues form (algo_lindblad_cvr_rodr.hpp:143-229,
+// coherence_vector_representation.hpp:52-213). The reference advances the
+// coherence vector d by
+//     d1 = A1 (d + d_in) - d_in,  d2 = A2(e) d1,  d = A1 (d2 + d_in) - d_in
+// with A1 = exp(M dt/2) and A2(e) = exp(e dt U), U skew-symmetric, A2 built
+// from the real-Schur planes of U. Here the state is kept in the basis Q of
+// those planes: z = Q^T (d + d_in). Then
+//     z <- B (R(e) (B z - c) + c),  B = Q^T A1 Q,  c = Q^T d_in,
+// where R(e) is block-diagonal with a 2x2 rotation by theta_k e dt per plane
+// and the identity on the null space of U: two V x V products and V/2 plane
+// rotations per point and step instead of forming A2. The polarisation
+// current p_t = M_CP v^T (M d + d_eq) becomes g^T z + p0 with
+// g = M_CP Q^T M^T v and p0 = M_CP v^T (d_eq - M d_in). B is stored as
+// B - I (computed from exp(X) - I directly), so that the FP32 kernels add a
+// small correction to an exact identity.
+//
+// Planes of U: U is real skew-symmetric, so i U is complex Hermitian with
+// eigenvalues +-theta_k; an eigenvector a + i b for +theta gives the
+// orthonormal pair q1 = sqrt2 a, q2 = sqrt2 b with U q1 = theta q2,
+// U q2 = -theta q1. Eigen-decomposition by the cyclic complex Jacobi method
+// (Golub & Van Loan, Matrix Computations, 4th ed., sec. 8.5, with the
+// complex phase rotation for Hermitian matrices); the null space is
+// completed by Gram-Schmidt against the unit vectors.
+//
+// Matrix exponential: scaling and squaring with a truncated Taylor series
+// (Moler & Van Loan, "Nineteen dubious ways to compute the exponential of
+// a matrix", method 3 with scaling and squaring), evaluated as exp(X) - I
+// and squared with F <- F (F + 2I) so that exp(X) - I keeps its relative
+// accuracy for small X.
+//
+// Regular / Cayley form (algo_lindblad_reg_cayley.hpp:123-203): the kernel
+// uses kappa H0 and kappa mu (kappa = dt/(2 hbar)), D1 - I with
+// D1 = exp(S dt/2), D2 - 1 = expm1(gamma dt/2), H0/hbar and n mu.
+#pragma once
+
+#include "common.cuh"
+
+namespace mbg {
+namespace pre {
+
+// One material, flattened (FP64, SI units). Operators are full N x N.
+struct mat_in {
+    int32_t N;           // 0: no quantum-mechanical description
+    int32_t relax_kind;  // MBG_RELAX_*
+    int32_t rho_levels;
+    int32_t rho_num_off;  // off-diagonal entries of the initial rho (<= 15 kept)
+    double eps_r, mu_r, overlap, losses;
+    double carrier_density;
+    double dt, dx;
+    double h_re[36], h_im[36];
+    double mu_re[36], mu_im[36];
+    double S[36];        // scattering, row-major
+    double deph[15];     // packed upper triangle, column-major order
+    double rho_diag[6];
+    double rho_off_re[15], rho_off_im[15];
+};
+
+struct cd {
+    double re, im;
+};
+MBG_HD cd cmake(double r, double i) { return cd{ r, i }; }
+MBG_HD cd cadd(cd a, cd b) { return cd{ a.re + b.re, a.im + b.im }; }
+MBG_HD cd csub(cd a, cd b) { return cd{ a.re - b.re, a.im - b.im }; }
+MBG_HD cd cmul(cd a, cd b)
+{
+    return cd{ a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re };
+}
+MBG_HD cd cconj(cd a) { return cd{ a.re, -a.im }; }
+
+// ------------------------------------------------------------- layouts
+
+// Constant block of one material for the coherence-vector kernels.
+struct cvr_layout {
+    int N, V, KP;
+    int a, b, cH, gam, has_qm, p0, nplanes;
+    int Bd, c, g, thdt, z0, inv, inv_c, pop, pop_c;
+    int Q;       // the plane basis (inspection only; kernels stop before it)
+    int stage;   // leading part a kernel stages in shared memory
+    int stride;
+};
+
+MBG_HD cvr_layout make_cvr_layout(int N)
+{
+    cvr_layout L;
+    L.N = N;
+    L.V = (N > 0) ? N * N - 1 : 0;
+    L.KP = L.V / 2;
+    L.a = 0;
+    L.b = 1;
+    L.cH = 2;
+    L.gam = 3;
+    L.has_qm = 4;
+    L.p0 = 5;
+    L.nplanes = 6;
+    int o = 8;
+    L.Bd = o;
+    o += L.V * L.V;
+    L.c = o;
+    o += L.V;
+    L.g = o;
+    o += L.V;
+    L.thdt = o;
+    o += (L.KP > 0 ? L.KP : 1);
+    L.z0 = o;
+    o += L.V;
+    L.inv = o;
+    o += L.V;
+    L.inv_c = o;
+    o += 1;
+    L.pop = o;
+    o += N * L.V;
+    L.pop_c = o;
+    o += N;
+    L.stage = (o + 3) & ~3;
+    L.Q = L.stage;
+    o = L.Q + L.V * L.V;
+    L.stride = (o + 3) & ~3;
+    return L;
+}
+
+// Constant block of one material for the Cayley kernels. Hermitian
+// operators are packed as N real diagonal entries followed by the upper
+// triangle in column-major order as (re, im) pairs: N^2 reals.
+struct cay_layout {
+    int N, P;
+    int a, b, cH, gam, has_qm;
+    int kH0, kMu, W0, Mn, dD1, d1, dD2, d2, rho0, stride;
+};
+
+MBG_HD cay_layout make_cay_layout(int N)
+{
+    cay_layout L;
+    L.N = N;
+    L.P = N * (N - 1) / 2;
+    L.a = 0;
+    L.b = 1;
+    L.cH = 2;
+    L.gam = 3;
+    L.has_qm = 4;
+    int o = 8;
+    L.kH0 = o;
+    o += N * N;
+    L.kMu = o;
+    o += N * N;
+    L.W0 = o;
+    o += N * N;
+    L.Mn = o;
+    o += N * N;
+    L.dD1 = o;
+    o += N * N;
+    L.d1 = o;
+    o += N * N;
+    L.dD2 = o;
+    o += (L.P > 0 ? L.P : 1);
+    L.d2 = o;
+    o += (L.P > 0 ? L.P : 1);
+    L.rho0 = o;
+    o += N * N;
+    L.stride = (o + 3) & ~3;
+    return L;
+}
+
+// Packed index of the upper off-diagonal entry (j, k), j < k, in
+// column-major order: (0,1), (0,2), (1,2), (0,3), ...
+MBG_HD int upper_index(int j, int k) { return k * (k - 1) / 2 + j; }
+
+// --------------------------------------------------------- small linalg
+
+// C = A * B, n x n row-major
+MBG_HD void mat_mul(const double* A, const double* B, double* C, int n)
+{
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) {
+            double s = 0.0;
+            for (int k = 0; k < n; k++) s += A[i * n + k] * B[k * n + j];
+            C[i * n + j] = s;
+        }
+}
+
+MBG_HD double norm1(const double* A, int n)
+{
+    double m = 0.0;
+    for (int j = 0; j < n; j++) {
+        double s = 0.0;
+        for (int i = 0; i < n; i++) s += fabs(A[i * n + j]);
+        m = s > m ? s : m;
+    }
+    return m;
+}
+
+// F = exp(X) - I by scaling and squaring of a truncated Taylor series.
+// ws: 3 n^2 doubles.
+MBG_HD void expm_minus_identity(const double* X, double* F, int n, double* ws)
+{
+    double* Y = ws;
+    double* T = ws + n * n;
+    double* W = ws + 2 * n * n;
+    double nrm = norm1(X, n);
+    int s = 0;
+    while (nrm > 0.25 && s < 200) {
+        nrm *= 0.5;
+        s++;
+    }
+    double scale = ldexp(1.0, -s);
+    for (int i = 0; i < n * n; i++) Y[i] = X[i] * scale;
+    // degree: smallest m with nrm^(m+1)/(m+1)! below 2^-60
+    int m = 1;
+    double term = nrm;
+    while (m < 24) {
+        term *= nrm / (m + 1);
+        if (term < 8.7e-19) break;
+        m++;
+    }
+    // F = Y (I + Y/2 (I + Y/3 (... (I + Y/m))))  (Horner form of e^Y - I)
+    for (int i = 0; i < n * n; i++) T[i] = 0.0;
+    for (int k = m; k >= 1; k--) {
+        // T <- Y (I + T) / k   (T holds the bracket without its identity)
+        for (int i = 0; i < n; i++) T[i * n + i] += 1.0;
+        mat_mul(Y, T, W, n);
+        for (int i = 0; i < n * n; i++) T[i] = W[i] / k;
+    }
+    for (int i = 0; i < n * n; i++) F[i] = T[i];
+    // squaring: e^{2Y} - I = F (F + 2 I)
+    for (int q = 0; q < s; q++) {
+        for (int i = 0; i < n * n; i++) T[i] = F[i];
+        for (int i = 0; i < n; i++) T[i * n + i] += 2.0;
+        mat_mul(F, T, W, n);
+        for (int i = 0; i < n * n; i++) F[i] = W[i];
+    }
+}
+
+// Solve A x = b by Gaussian elimination with partial pivoting (A, b are
+// overwritten). Returns 0, or 1 if a pivot is exactly zero.
+MBG_HD int solve_partial_pivot(double* A, double* b, double* x, int n)
+{
+    int singular = 0;
+    for (int k = 0; k < n; k++) {
+        int p = k;
+        for (int i = k + 1; i < n; i++)
+            if (fabs(A[i * n + k]) > fabs(A[p * n + k])) p = i;
+        if (p != k) {
+            for (int j = 0; j < n; j++) {
+                double t = A[k * n + j];
+                A[k * n + j] = A[p * n + j];
+                A[p * n + j] = t;
+            }
+            double t = b[k];
+            b[k] = b[p];
+            b[p] = t;
+        }
+        double piv = A[k * n + k];
+        if (piv == 0.0) {
+            singular = 1;
+            continue;
+        }
+        for (int i = k + 1; i < n; i++) {
+            double f = A[i * n + k] / piv;
+            for (int j = k; j < n; j++) A[i * n + j] -= f * A[k * n + j];
+            b[i] -= f * b[k];
+        }
+    }
+    for (int k = n - 1; k >= 0; k--) {
+        double piv = A[k * n + k];
+        if (piv == 0.0) {
+            x[k] = 0.0;
+            continue;
+        }
+        double s = b[k];
+        for (int j = k + 1; j < n; j++) s -= A[k * n + j] * x[j];
+        x[k] = s / piv;
+    }
+    return singular;
+}
+
+// Cyclic Jacobi eigen-decomposition of a complex Hermitian n x n matrix
+// (re/im row-major, overwritten; the diagonal ends as the eigenvalues).
+// Eigenvectors are the columns of (vre, vim).
+MBG_HD void jacobi_hermitian(
+    double* are,
+    double* aim,
+    double* vre,
+    double* vim,
+    int n)
+{
+    for (int i = 0; i < n * n; i++) {
+        vre[i] = (i % (n + 1) == 0) ? 1.0 : 0.0;
+        vim[i] = 0.0;
+    }
+    for (int sweep = 0; sweep < 60; sweep++) {
+        double off = 0.0, tot = 0.0;
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) {
+                double m2 = are[i * n + j] * are[i * n + j] +
+                    aim[i * n + j] * aim[i * n + j];
+                tot += m2;
+                if (i != j) off += m2;
+            }
+        if (off <= 1e-32 * tot) break;
+        for (int p = 0; p < n - 1; p++)
+            for (int q = p + 1; q < n; q++) {
+                double zr = are[p * n + q], zi = aim[p * n + q];
+                double r = sqrt(zr * zr + zi * zi);
+                if (r == 0.0) continue;
+                double ephr = zr / r, ephi = zi / r;  // e^{i phi}
+                double app = are[p * n + p], aqq = are[q * n + q];
+                double tau = (aqq - app) / (2.0 * r);
+                double t = (tau >= 0 ? 1.0 : -1.0) /
+                    (fabs(tau) + sqrt(1.0 + tau * tau));
+                double c = 1.0 / sqrt(1.0 + t * t), s = t * c;
+                // J = [[c, s], [-s e^{-i phi}, c e^{-i phi}]] on (p, q)
+                // columns: X <- X J
+                for (int k = 0; k < n; k++) {
+                    double xpr = are[k * n + p], xpi = aim[k * n + p];
+                    double xqr = are[k * n + q], xqi = aim[k * n + q];
+                    // e^{-i phi} x_q
+                    double yr = ephr * xqr + ephi * xqi;
+                    double yi = ephr * xqi - ephi * xqr;
+                    are[k * n + p] = c * xpr - s * yr;
+                    aim[k * n + p] = c * xpi - s * yi;
+                    are[k * n + q] = s * xpr + c * yr;
+                    aim[k * n + q] = s * xpi + c * yi;
+                }
+                // rows: X <- J^H X
+                for (int k = 0; k < n; k++) {
+                    double xpr = are[p * n + k], xpi = aim[p * n + k];
+                    double xqr = are[q * n + k], xqi = aim[q * n + k];
+                    // e^{+i phi} x_q
+                    double yr = ephr * xqr - ephi * xqi;
+                    double yi = ephr * xqi + ephi * xqr;
+                    are[p * n + k] = c * xpr - s * yr;
+                    aim[p * n + k] = c * xpi - s * yi;
+                    are[q * n + k] = s * xpr + c * yr;
+                    aim[q * n + k] = s * xpi + c * yi;
+                }
+                are[p * n + q] = aim[p * n + q] = 0.0;
+                are[q * n + p] = aim[q * n + p] = 0.0;
+                aim[p * n + p] = aim[q * n + q] = 0.0;
+                for (int k = 0; k < n; k++) {
+                    double xpr = vre[k * n + p], xpi = vim[k * n + p];
+                    double xqr = vre[k * n + q], xqi = vim[k * n + q];
+                    double yr = ephr * xqr + ephi * xqi;
+                    double yi = ephr * xqi - ephi * xqr;
+                    vre[k * n + p] = c * xpr - s * yr;
+                    vim[k * n + p] = c * xpi - s * yi;
+                    vre[k * n + q] = s * xpr + c * yr;
+                    vim[k * n + q] = s * xpi + c * yi;
+                }
+            }
+    }
+}
+
+// --------------------------------------------------- SU(N) generators
+
+// Sparse entries of generator i of su(N) in the reference's order
+// (coherence_vector_representation.hpp:52-93): u_jk, then v_jk, then w_l.
+MBG_HD int generator_entries(int N, int i, int* r, int* c, cd* v)
+{
+    int P = N * (N - 1) / 2;
+    if (i < 2 * P) {
+        int p = (i < P) ? i : i - P;
+        int k = 1;
+        while (k * (k + 1) / 2 <= p) k++;
+        int j = p - k * (k - 1) / 2;
+        r[0] = j;
+        c[0] = k;
+        r[1] = k;
+        c[1] = j;
+        if (i < P) {
+            v[0] = cmake(1, 0);
+            v[1] = cmake(1, 0);
+        } else {
+            v[0] = cmake(0, -1);
+            v[1] = cmake(0, 1);
+        }
+        return 2;
+    }
+    int l = i - 2 * P;
+    double nrm = 1.0 / sqrt((double) (((l + 1) * (l + 2)) / 2));
+    int cnt = 0;
+    for (int j = 0; j <= l; j++) {
+        r[cnt] = j;
+        c[cnt] = j;
+        v[cnt] = cmake(-nrm, 0);
+        cnt++;
+    }
+    r[cnt] = l + 1;
+    c[cnt] = l + 1;
+    v[cnt] = cmake((l + 1) * nrm, 0);
+    return cnt + 1;
+}
+
+// tr(A g) for dense A (N x N complex) and sparse generator g
+MBG_HD cd trace_with_gen(
+    const double* are,
+    const double* aim,
+    int N,
+    int nz,
+    const int* r,
+    const int* c,
+    const cd* v)
+{
+    cd s = cmake(0, 0);
+    for (int e = 0; e < nz; e++) {
+        cd a = cmake(are[c[e] * N + r[e]], aim[c[e] * N + r[e]]);
+        s = cadd(s, cmul(a, v[e]));
+    }
+    return s;
+}
+
+// Lindblad relaxation action on a Hermitian matrix (qm_description.hpp:
+// 211-236); the base superoperator (relax_kind 0) returns zero.
+MBG_HD void relax_apply(
+    const mat_in& m,
+    const double* xre,
+    const double* xim,
+    double* yre,
+    double* yim)
+{
+    int N = m.N;
+    for (int i = 0; i < N * N; i++) yre[i] = yim[i] = 0.0;
+    if (m.relax_kind != 1) return;
+    for (int a = 0; a < N; a++) {
+        double s = 0.0;
+        for (int b = 0; b < N; b++) s += m.S[a * N + b] * xre[b * N + b];
+        yre[a * N + a] = s;
+    }
+    for (int k = 1; k < N; k++)
+        for (int j = 0; j < k; j++) {
+            double d = m.deph[upper_index(j, k)];
+            double zr = xre[j * N + k] * d, zi = xim[j * N + k] * d;
+            yre[j * N + k] = zr;
+            yim[j * N + k] = zi;
+            yre[k * N + j] = zr;
+            yim[k * N + j] = -zi;
+        }
+}
+
+// Coherence vector of the initial density matrix exactly as
+// coherence_vector_representation.hpp:341-394 computes it (including its
+// indexing: every off-diagonal entry writes the first slot of its block,
+// so only the last entry's value is kept there).
+MBG_HD void initial_coherence_vector(const mat_in& m, double* d)
+{
+    int N = m.N, V = N * N - 1, P = N * (N - 1) / 2;
+    for (int i = 0; i < V; i++) d[i] = 0.0;
+    int rn = m.rho_levels;
+    int rp = m.rho_num_off;
+    for (int j = 0; j < rp; j++) d[0] = 2 * m.rho_off_re[j];
+    for (int j = 0; j < rp; j++) d[P] = -2 * m.rho_off_im[j];
+    for (int l = 0; l < N - 1; l++) {
+        double e = 0.0;
+        int j = 0;
+        for (j = 0; j <= l; j++) e += -1.0 * (j < rn ? m.rho_diag[j] : 0.0);
+        e += (l + 1) * (j < rn ? m.rho_diag[j] : 0.0);
+        d[2 * P + l] = e / sqrt((double) (((l + 1) * (l + 2)) / 2));
+    }
+}
+
+// Population weights of coherence_vector_representation.hpp:289-336:
+// rho_mm = 1/N + 1/2 sum_i w_i d[N(N-1) + i].
+MBG_HD double population_weight(int N, int m, int i)
+{
+    if (N == 3 && m > 2) return 0.0;
+    double f;
+    if (m < i + 1)
+        f = -1.0;
+    else if (m == i + 1)
+        f = (double) m;
+    else
+        f = 0.0;
+    return f / sqrt((double) (((i + 1) * (i + 2)) / 2));
+}
+MBG_HD double population_const(int N, int m)
+{
+    return (N == 3 && m > 2) ? 0.0 : 1.0 / N;
+}
+
+// Workspace doubles needed by cvr_precompute for N levels.
+MBG_HD size_t cvr_workspace(int N)
+{
+    size_t V = (size_t) N * N - 1;
+    return V * N * N * 2 + V * V * 14 + V * 12 + 64;
+}
+
+// FDTD constants (common_fdtd.hpp:158-190).
+MBG_HD void fdtd_constants(const mat_in& m, double* a, double* b, double* c)
+{
+    double sigma = sqrt(EPS0 * m.eps_r / (MU0 * m.mu_r)) * m.losses * 2.0;
+    double epsilon = EPS0 * m.eps_r;
+    double x = (sigma * m.dt) / (2.0 * epsilon);
+    *a = (1.0 - x) / (1.0 + x);
+    *b = m.dt / epsilon / (1.0 + x);
+    *c = m.dt / (MU0 * m.mu_r * m.dx);
+}
+
+// Coherence-vector constants of one material into out (cvr_layout of
+// `Nsolver` levels). Returns 0 on success, 1 when the level count does not
+// match the solver, 2 when M d_in = d_eq has no solution (the reference's
+// "Time-indepent matrix not invertible!" check, rodr.hpp:195-206).
+MBG_HD int cvr_precompute(const mat_in& m, int Nsolver, double* ws, double* out)
+{
+    cvr_layout L = make_cvr_layout(Nsolver);
+    for (int i = 0; i < L.stride; i++) out[i] = 0.0;
+    double a, b, c;
+    fdtd_constants(m, &a, &b, &c);
+    out[L.a] = a;
+    out[L.b] = b;
+    out[L.cH] = c;
+    out[L.gam] = m.overlap;
+    const int N = Nsolver, V = L.V, KP = L.KP;
+    if (m.N == 0) {
+        // no quantum-mechanical description: the density stays the zero
+        // vector, whose populations are 1/N (cvr.hpp:289-336)
+        out[L.has_qm] = 0.0;
+        for (int k = 0; k < N; k++) out[L.pop_c + k] = population_const(N, k);
+        return 0;
+    }
+    if (m.N != Nsolver) return 1;
+    out[L.has_qm] = 1.0;
+    const int NN = N * N;
+    double* X = ws;                        // V * N*N * 2 : op * g_i
+    double* Tr = X + (size_t) V * NN * 2;  // V*V*2 : tr(op g_i g_j)
+    double* M = Tr + V * V * 2;
+    double* U = M + V * V;
+    double* F = U + V * V;
+    double* Q = F + V * V;
+    double* H1 = Q + V * V;   // Hermitian re
+    double* H2 = H1 + V * V;  // Hermitian im
+    double* E1 = H2 + V * V;  // eigvec re
+    double* E2 = E1 + V * V;  // eigvec im
+    double* W = E2 + V * V;   // 3 V*V expm workspace
+    double* vec = W + 3 * V * V;
+    double* v_dip = vec;
+    double* d_eq = vec + V;
+    double* d_in = vec + 2 * V;
+    double* t1 = vec + 3 * V;
+    double* t2 = vec + 4 * V;
+    double* lam = vec + 5 * V;
+    double* d0 = vec + 6 * V;
+    double* tre = vec + 7 * V;  // N*N (<= V+1)
+    double* tim = tre + NN;
+    double* ure = tim + NN;
+    double* uim = ure + NN;
+
+    int gr[8], gc[8];
+    cd gv[8];
+    // Liouvillians L(op)_ij = Re(i/2 tr(op [g_i, g_j])) / hbar
+    // (coherence_vector_representation.hpp:149-166) of H and mu
+    for (int which = 0; which < 2; which++) {
+        const double* ore = which == 0 ? m.h_re : m.mu_re;
+        const double* oim = which == 0 ? m.h_im : m.mu_im;
+        for (int i = 0; i < V; i++) {
+            int nz = generator_entries(N, i, gr, gc, gv);
+            double* xr = X + (size_t) i * NN * 2;
+            double* xi = xr + NN;
+            for (int e = 0; e < NN; e++) xr[e] = xi[e] = 0.0;
+            // (op g)(r', c) = sum over entries g(r, c): op(r', r) g(r, c)
+            for (int e = 0; e < nz; e++)
+                for (int rr = 0; rr < N; rr++) {
+                    cd o = cmake(ore[rr * N + gr[e]], oim[rr * N + gr[e]]);
+                    cd p = cmul(o, gv[e]);
+                    xr[rr * N + gc[e]] += p.re;
+                    xi[rr * N + gc[e]] += p.im;
+                }
+        }
+        for (int i = 0; i < V; i++)
+            for (int j = 0; j < V; j++) {
+                int nz = generator_entries(N, j, gr, gc, gv);
+                const double* xr = X + (size_t) i * NN * 2;
+                cd t = trace_with_gen(xr, xr + NN, N, nz, gr, gc, gv);
+                Tr[(i * V + j) * 2] = t.re;
+                Tr[(i * V + j) * 2 + 1] = t.im;
+            }
+        for (int i = 0; i < V; i++)
+            for (int j = 0; j < V; j++) {
+                double dim = Tr[(i * V + j) * 2 + 1] - Tr[(j * V + i) * 2 + 1];
+                double l = -0.5 * dim / HBAR;  // Re(i z / 2) = -Im(z) / 2
+                if (which == 0)
+                    M[i * V + j] = l;
+                else
+                    U[i * V + j] = -l;  // U = -L(mu)
+            }
+        if (which == 1) {
+            // dipole vector v_i = Re tr(mu g_i) (cvr.hpp:168-179)
+            for (int i = 0; i < V; i++) {
+                int nz = generator_entries(N, i, gr, gc, gv);
+                v_dip[i] = trace_with_gen(m.mu_re, m.mu_im, N, nz, gr, gc, gv).re;
+            }
+        }
+    }
+    // relaxation superoperator G_ij = Re 1/2 tr(R(g_j) g_i) and the
+    // equilibrium vector d_eq_i = Re tr(R(I) g_i) / N (cvr.hpp:181-213)
+    for (int j = 0; j < V; j++) {
+        int nz = generator_entries(N, j, gr, gc, gv);
+        for (int e = 0; e < NN; e++) tre[e] = tim[e] = 0.0;
+        for (int e = 0; e < nz; e++) {
+            tre[gr[e] * N + gc[e]] = gv[e].re;
+            tim[gr[e] * N + gc[e]] = gv[e].im;
+        }
+        relax_apply(m, tre, tim, ure, uim);
+        for (int i = 0; i < V; i++) {
+            int nzi = generator_entries(N, i, gr, gc, gv);
+            cd t = trace_with_gen(ure, uim, N, nzi, gr, gc, gv);
+            M[i * V + j] += 0.5 * t.re;
+        }
+    }
+    for (int e = 0; e < NN; e++) {
+        tre[e] = (e % (N + 1) == 0) ? 1.0 : 0.0;
+        tim[e] = 0.0;
+    }
+    relax_apply(m, tre, tim, ure, uim);
+    for (int i = 0; i < V; i++) {
+        int nz = generator_entries(N, i, gr, gc, gv);
+        d_eq[i] = trace_with_gen(ure, uim, N, nz, gr, gc, gv).re / N;
+    }
+    const double M_CP = 0.5 * m.carrier_density;
+
+    // d_in: M d_in = d_eq unless d_eq is zero (rodr.hpp:193-206)
+    bool zero = true;
+    for (int i = 0; i < V; i++)
+        if (fabs(d_eq[i]) > 2.220446049250313e-16) zero = false;
+    if (zero) {
+        for (int i = 0; i < V; i++) d_in[i] = 0.0;
+    } else {
+        for (int i = 0; i < V * V; i++) F[i] = M[i];
+        for (int i = 0; i < V; i++) t1[i] = d_eq[i];
+        solve_partial_pivot(F, t1, d_in, V);
+        double nr = 0.0, nd = 0.0;
+        for (int i = 0; i < V; i++) {
+            double s = -d_eq[i];
+            for (int j = 0; j < V; j++) s += M[i * V + j] * d_in[j];
+            nr += s * s;
+            nd += d_eq[i] * d_eq[i];
+        }
+        if (!(sqrt(nr) / sqrt(nd) <= 1e-3)) return 2;
+    }
+
+    // F = exp(M dt/2) - I
+    for (int i = 0; i < V * V; i++) H1[i] = M[i] * m.dt / 2;
+    expm_minus_identity(H1, F, V, W);
+
+    // planes of U from the Hermitian matrix i U
+    for (int i = 0; i < V * V; i++) {
+        H1[i] = 0.0;
+        H2[i] = U[i];
+    }
+    jacobi_hermitian(H1, H2, E1, E2, V);
+    for (int i = 0; i < V; i++) lam[i] = H1[i * V + i];
+    double lmax = 0.0;
+    for (int i = 0; i < V; i++) lmax = lam[i] > lmax ? lam[i] : lmax;
+    int used[64];
+    for (int i = 0; i < V; i++) used[i] = 0;
+    int ncol = 0, nplanes = 0;
+    while (nplanes < KP) {
+        int best = -1;
+        for (int i = 0; i < V; i++)
+            if (!used[i] && lam[i] > 1e-9 * lmax && lmax > 0.0 &&
+                (best < 0 || lam[i] > lam[best]))
+                best = i;
+        if (best < 0) break;
+        used[best] = 1;
+        // q1, q2 from the real and imaginary parts, re-orthonormalised
+        double n1 = 0.0;
+        for (int i = 0; i < V; i++) {
+            t1[i] = E1[i * V + best];
+            t2[i] = E2[i * V + best];
+        }
+        for (int pass = 0; pass < 2; pass++)
+            for (int col = 0; col < ncol; col++) {
+                double d1 = 0.0, d2 = 0.0;
+                for (int i = 0; i < V; i++) {
+                    d1 += Q[i * V + col] * t1[i];
+                    d2 += Q[i * V + col] * t2[i];
+                }
+                for (int i = 0; i < V; i++) {
+                    t1[i] -= d1 * Q[i * V + col];
+                    t2[i] -= d2 * Q[i * V + col];
+                }
+            }
+        for (int i = 0; i < V; i++) n1 += t1[i] * t1[i];
+        n1 = sqrt(n1);
+        if (n1 < 1e-3) continue;
+        for (int i = 0; i < V; i++) t1[i] /= n1;
+        double dd = 0.0;
+        for (int i = 0; i < V; i++) dd += t1[i] * t2[i];
+        double n2 = 0.0;
+        for (int i = 0; i < V; i++) {
+            t2[i] -= dd * t1[i];
+            n2 += t2[i] * t2[i];
+        }
+        n2 = sqrt(n2);
+        if (n2 < 1e-3) continue;
+        for (int i = 0; i < V; i++) t2[i] /= n2;
+        // theta = q2 . U q1 ; orient so that theta > 0
+        double th = 0.0;
+        for (int i = 0; i < V; i++) {
+            double s = 0.0;
+            for (int j = 0; j < V; j++) s += U[i * V + j] * t1[j];
+            th += t2[i] * s;
+        }
+        if (th < 0) {
+            th = -th;
+            for (int i = 0; i < V; i++) t2[i] = -t2[i];
+        }
+        for (int i = 0; i < V; i++) {
+            Q[i * V + ncol] = t1[i];
+            Q[i * V + ncol + 1] = t2[i];
+        }
+        out[L.thdt + nplanes] = th * m.dt;
+        ncol += 2;
+        nplanes++;
+    }
+    out[L.nplanes] = nplanes;
+    // complete Q with an orthonormal basis of the null space of U
+    while (ncol < V) {
+        int best = -1;
+        double bestn = -1.0;
+        for (int i = 0; i < V; i++) {
+            double s = 1.0;
+            for (int col = 0; col < ncol; col++)
+                s -= Q[i * V + col] * Q[i * V + col];
+            if (s > bestn) {
+                bestn = s;
+                best = i;
+            }
+        }
+        for (int i = 0; i < V; i++) t1[i] = (i == best) ? 1.0 : 0.0;
+        for (int pass = 0; pass < 2; pass++)
+            for (int col = 0; col < ncol; col++) {
+                double d = 0.0;
+                for (int i = 0; i < V; i++) d += Q[i * V + col] * t1[i];
+                for (int i = 0; i < V; i++) t1[i] -= d * Q[i * V + col];
+            }
+        double nn = 0.0;
+        for (int i = 0; i < V; i++) nn += t1[i] * t1[i];
+        nn = sqrt(nn);
+        for (int i = 0; i < V; i++) Q[i * V + ncol] = t1[i] / nn;
+        ncol++;
+    }
+
+    for (int i = 0; i < V * V; i++) out[L.Q + i] = Q[i];
+    // Bd = Q^T F Q   (= Q^T A1 Q - I)
+    for (int i = 0; i < V; i++)
+        for (int j = 0; j < V; j++) {
+            double s = 0.0;
+            for (int k = 0; k < V; k++) s += F[i * V + k] * Q[k * V + j];
+            H1[i * V + j] = s;  // F Q
+        }
+    for (int i = 0; i < V; i++)
+        for (int j = 0; j < V; j++) {
+            double s = 0.0;
+            for (int k = 0; k < V; k++) s += Q[k * V + i] * H1[k * V + j];
+            out[L.Bd + i * V + j] = s;
+        }
+    // c = Q^T d_in ; g = M_CP Q^T M^T v ; p0 = M_CP v^T (d_eq - M d_in)
+    for (int j = 0; j < V; j++) {
+        double s = 0.0;
+        for (int i = 0; i < V; i++) s += M[i * V + j] * v_dip[i];
+        t1[j] = s;  // (M^T v)_j
+    }
+    double p0 = 0.0;
+    for (int i = 0; i < V; i++) {
+        double s = d_eq[i];
+        for (int j = 0; j < V; j++) s -= M[i * V + j] * d_in[j];
+        p0 += v_dip[i] * s;
+    }
+    out[L.p0] = M_CP * p0;
+    for (int k = 0; k < V; k++) {
+        double sc = 0.0, sg = 0.0;
+        for (int i = 0; i < V; i++) {
+            sc += Q[i * V + k] * d_in[i];
+            sg += Q[i * V + k] * t1[i];
+        }
+        out[L.c + k] = sc;
+        out[L.g + k] = M_CP * sg;
+    }
+    // initial state z0 = Q^T (d0 + d_in)
+    initial_coherence_vector(m, d0);
+    for (int k = 0; k < V; k++) {
+        double s = 0.0;
+        for (int i = 0; i < V; i++) s += Q[i * V + k] * (d0[i] + d_in[i]);
+        out[L.z0 + k] = s;
+    }
+    // observables: d = Q z - d_in
+    int w0 = N * (N - 1);
+    for (int k = 0; k < V; k++) out[L.inv + k] = Q[w0 * V + k];
+    out[L.inv_c] = -d_in[w0];
+    for (int mm = 0; mm < N; mm++) {
+        double cst = population_const(N, mm);
+        for (int k = 0; k < V; k++) out[L.pop + mm * V + k] = 0.0;
+        for (int i = 0; i < N - 1; i++) {
+            double w = 0.5 * population_weight(N, mm, i);
+            for (int k = 0; k < V; k++)
+                out[L.pop + mm * V + k] += w * Q[(w0 + i) * V + k];
+            cst -= w * d_in[w0 + i];
+        }
+        out[L.pop_c + mm] = cst;
+    }
+    return 0;
+}
+
+// Workspace doubles needed by cay_precompute.
+MBG_HD size_t cay_workspace(int N) { return (size_t) N * N * 5 + 16; }
+
+MBG_HD void pack_hermitian(const double* re, const double* im, int N, double s, double* out)
+{
+    for (int i = 0; i < N; i++) out[i] = re[i * N + i] * s;
+    for (int k = 1; k < N; k++)
+        for (int j = 0; j < k; j++) {
+            int p = upper_index(j, k);
+            out[N + 2 * p] = re[j * N + k] * s;
+            out[N + 2 * p + 1] = im[j * N + k] * s;
+        }
+}
+
+// Cayley constants of one material (cay_layout of `Nsolver` levels).
+// Returns 0, 1 on a level-count mismatch, 3 for a relaxation superoperator
+// that is not of Lindblad form (reg_cayley.hpp:146-155).
+MBG_HD int cay_precompute(const mat_in& m, int Nsolver, double* ws, double* out)
+{
+    cay_layout L = make_cay_layout(Nsolver);
+    for (int i = 0; i < L.stride; i++) out[i] = 0.0;
+    double a, b, c;
+    fdtd_constants(m, &a, &b, &c);
+    out[L.a] = a;
+    out[L.b] = b;
+    out[L.cH] = c;
+    out[L.gam] = m.overlap;
+    int N = Nsolver;
+    if (m.N == 0) {
+        out[L.has_qm] = 0.0;
+        return 0;
+    }
+    if (m.N != Nsolver) return 1;
+    if (m.relax_kind != 1) return 3;
+    out[L.has_qm] = 1.0;
+    const double kappa = m.dt / (2.0 * HBAR);
+    pack_hermitian(m.h_re, m.h_im, N, kappa, out + L.kH0);
+    pack_hermitian(m.mu_re, m.mu_im, N, kappa, out + L.kMu);
+    pack_hermitian(m.h_re, m.h_im, N, 1.0 / HBAR, out + L.W0);
+    pack_hermitian(m.mu_re, m.mu_im, N, m.carrier_density, out + L.Mn);
+    double* X = ws;
+    double* Fm = ws + N * N;
+    double* W = ws + 2 * N * N;
+    for (int i = 0; i < N * N; i++) X[i] = m.S[i] * m.dt / 2;
+    expm_minus_identity(X, Fm, N, W);
+    for (int i = 0; i < N * N; i++) {
+        out[L.dD1 + i] = Fm[i];
+        out[L.d1 + i] = m.S[i];
+    }
+    for (int p = 0; p < L.P; p++) {
+        out[L.dD2 + p] = expm1(m.deph[p] * m.dt / 2);
+        out[L.d2 + p] = m.deph[p];
+    }
+    // initial density matrix (reg_cayley.hpp:269-272)
+    int rn = m.rho_levels;
+    for (int i = 0; i < N; i++) out[L.rho0 + i] = i < rn ? m.rho_diag[i] : 0.0;
+    for (int p = 0; p < L.P && p < m.rho_num_off; p++) {
+        out[L.rho0 + N + 2 * p] = m.rho_off_re[p];
+        out[L.rho0 + N + 2 * p + 1] = m.rho_off_im[p];
+    }
+    return 0;
+}
+
+// FDTD-only constants (Maxwell solver, algo_lindblad_noop.hpp)
+MBG_HD int noop_precompute(const mat_in& m, double* out)
+{
+    cvr_layout L = make_cvr_layout(0);
+    for (int i = 0; i < L.stride; i++) out[i] = 0.0;
+    double a, b, c;
+    fdtd_constants(m, &a, &b, &c);
+    out[L.a] = a;
+    out[L.b] = b;
+    out[L.cH] = c;
+    out[L.gam] = m.overlap;
+    return 0;
+}
+
+}  // namespace pre
+}  // namespace mbg

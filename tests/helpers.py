@@ -1,0 +1,74 @@
+"""Shared test helpers: run a (device, scenario) on the oracle, on the
+reference-built library and on the GPU engine, and compare results."""
+import ctypes as C
+import json
+import os
+
+import numpy as np
+
+from mbsolve_gb300 import capi_types as T
+from mbsolve_gb300 import lib as mb
+from mbsolve_gb300 import setups
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def build_setup(spec):
+    """(device, scenario) from a JSON-able spec {"setup": name, "kw": {}}."""
+    fn = getattr(setups, spec["setup"])
+    return fn(**spec.get("kw", {}))
+
+
+def oracle_results(algo, num_levels, dev, sce, threads=2, max_steps=0):
+    from oracle import oracle as O
+    b = mb.to_pod(dev, sce)
+    o = O.OracleRun(algo, num_levels, b)
+    o.run(threads=threads, max_steps=max_steps)
+    return o.grid(), [r for r, _ in o.results()]
+
+
+def reference_results(name, dev, sce):
+    from oracle import oracle as O
+    b = mb.to_pod(dev, sce)
+    r = O.ReferenceRun(name, b)
+    r.run()
+    return r.grid(), [x for x, _ in r.results(len(sce.get_records()))]
+
+
+def gpu_results(name, dev, sce, tuning=None):
+    from mbsolve_gb300 import solvergpu
+    s = solvergpu.solver_gpu_fdtd(dev, sce, name, tuning)
+    s.run()
+    return s._grid, [r.as_array() for r in s.get_results()]
+
+
+def rel_err(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    den = np.linalg.norm(b.ravel())
+    num = np.linalg.norm((a - b).ravel())
+    if den == 0.0:
+        return num
+    return num / den
+
+
+def load_golden(case):
+    d = np.load(os.path.join(GOLDEN, case + ".npz"))
+    meta = json.loads(str(d["meta"]))
+    recs = [d["rec%d" % k] for k in range(meta["num_records"])]
+    return meta, recs
+
+
+def golden_cases():
+    if not os.path.isdir(GOLDEN):
+        return []
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+
+
+def tuning(C_=0, NT=0, depth=0, graph=0):
+    t = T.mbg_tuning()
+    t.cells_per_thread = C_
+    t.threads = NT
+    t.depth = depth
+    t.launches_per_graph = graph
+    return t

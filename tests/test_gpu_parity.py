@@ -1,0 +1,173 @@
+"""GPU parity through the C-ABI: every golden case (the reference's own
+time loop) in FP64 and FP32, tuning invariance (temporal blocking depth,
+tile shape) bit for bit, ensembles against single runs, error paths."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from mbsolve_gb300 import capi_types as T
+from mbsolve_gb300 import lib as mb
+from mbsolve_gb300 import setups
+from tests import helpers
+
+pytestmark = pytest.mark.gpu
+
+# relative L2 error per record against the reference's FP64 result
+TOL = {"fp64": 1e-9, "fp32": 2e-4}
+
+
+def _gpu_name(cpu_name, prec):
+    return cpu_name.replace("cpu-", "gpu-") + "-" + prec
+
+
+def _check(a, b, tol, what):
+    nb = np.linalg.norm(b)
+    err = np.linalg.norm(a - b)
+    if nb == 0.0:
+        assert err <= 1e-300 or err <= tol * 1e-6, (what, err)
+        return 0.0
+    assert err <= tol * nb, (what, err / nb)
+    return err / nb
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("case", helpers.golden_cases())
+def test_gpu_matches_golden(native, case, prec):
+    meta, recs = helpers.load_golden(case)
+    dev, sce = helpers.build_setup(meta["spec"])
+    grid, res = helpers.gpu_results(_gpu_name(meta["solver"], prec), dev, sce)
+    assert grid.num_timesteps == meta["num_timesteps"]
+    assert sce.get_timestep_size() == meta["timestep_size"]
+    errs = []
+    for k, (a, b) in enumerate(zip(res, recs)):
+        assert a.shape == b.shape
+        errs.append(_check(a, b, TOL[prec], (case, k)))
+    print(case, prec, ["%.2e" % e for e in errs])
+
+
+@pytest.mark.parametrize("name,setup,kw", [
+    ("gpu-fdtd-2lvl-cvr-rodr-fp32", "sit_2lvl",
+     dict(num_gridpoints=3000, num_timesteps=700)),
+    ("gpu-fdtd-2lvl-cvr-rodr-fp64", "sit_2lvl",
+     dict(num_gridpoints=3000, num_timesteps=700)),
+    ("gpu-fdtd-3lvl-reg-cayley-fp32", "lambda_3lvl",
+     dict(num_gridpoints=2000, num_timesteps=500)),
+    ("gpu-fdtd-2lvl-cvr-rodr-fp32", "ziolkowski1995",
+     dict(num_gridpoints=2500, endtime=40e-15)),
+])
+def test_tuning_does_not_change_results(native, name, setup, kw):
+    """Temporal blocking depth and tile shape change only the schedule:
+    results are bit-identical (a halo error would show here)."""
+    shapes = [(1, 128, 1, 2), (2, 128, 8, 4), (4, 256, 16, 8),
+              (8, 256, 32, 2), (1, 128, 24, 2), (2, 256, 5, 0)]
+    out = []
+    for c_, nt, d, g in shapes:
+        mb.material.clear_library()
+        dev, sce = helpers.build_setup({"setup": setup, "kw": kw})
+        t = helpers.tuning(c_, nt, d, g)
+        try:
+            _, res = helpers.gpu_results(name, dev, sce, t)
+        except Exception as e:  # shape not instantiated for this algo
+            if "no kernel instantiated" in str(e):
+                continue
+            raise
+        out.append(res)
+    assert len(out) >= 3
+    for res in out[1:]:
+        for a, b in zip(res, out[0]):
+            assert np.array_equal(a, b)
+
+
+def test_run_twice_continues_like_reference(native):
+    from oracle import oracle as O
+    dev, sce = setups.ziolkowski1995(1024, 30e-15)
+    b = mb.to_pod(dev, sce)
+    o = O.OracleRun("cvr-rodr", 2, b)
+    o.run(threads=2)
+    o.run(threads=2)
+    ref = [r for r, _ in o.results()]
+    mb.material.clear_library()
+    dev, sce = setups.ziolkowski1995(1024, 30e-15)
+    from mbsolve_gb300 import solvergpu
+    s = solvergpu.solver_gpu_fdtd(dev, sce, "gpu-fdtd-2lvl-cvr-rodr-fp64")
+    s.run()
+    s.run()
+    for a, r in zip(s.get_results(), ref):
+        _check(a.as_array(), r, 1e-9, "run twice")
+
+
+def _ensemble_runs():
+    runs = []
+    for n, area, det, t2 in [(700, 2.0, 0.0, 1e-9), (2500, 6.0, 0.03, 1e-12),
+                             (1201, 3.0, -0.04, 3e-13), (64, 9.0, 0.01, 1e-11)]:
+        runs.append(("sit_2lvl", dict(num_gridpoints=n, num_timesteps=900,
+                                      area=area, detuning=det, t2=t2)))
+    runs.append(("ziolkowski1995", dict(num_gridpoints=1500, endtime=40e-15)))
+    return runs
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_ensemble_equals_single_runs(native, prec):
+    from mbsolve_gb300 import ensemble
+    specs = _ensemble_runs()
+    pairs = [helpers.build_setup({"setup": s, "kw": kw}) for s, kw in specs]
+    ens = ensemble.ensemble("gpu-fdtd-2lvl-cvr-rodr-" + prec, pairs)
+    ens.run()
+    assert ens.status() == 0
+    for i, (s, kw) in enumerate(specs):
+        mb.material.clear_library()
+        dev, sce = helpers.build_setup({"setup": s, "kw": kw})
+        _, single = helpers.gpu_results("gpu-fdtd-2lvl-cvr-rodr-" + prec,
+                                        dev, sce)
+        got = [r.as_array() for r in ens.results(i)]
+        for a, b in zip(got, single):
+            assert np.array_equal(a, b)
+        if prec == "fp64":
+            mb.material.clear_library()
+            dev, sce = helpers.build_setup({"setup": s, "kw": kw})
+            _, orc = helpers.oracle_results("cvr-rodr", 2, dev, sce)
+            for a, b in zip(got, orc):
+                _check(a, b, 1e-9, ("ensemble", i))
+
+
+def test_device_precompute_equals_host(native):
+    from mbsolve_gb300 import _native
+    for N in (2, 3, 6):
+        dev, sce = setups.random_nlvl(N=N, num_gridpoints=16,
+                                      num_timesteps=10, seed=N)
+        b = mb.to_pod(dev, sce)
+        mat = b.device.materials[0]
+        n = C.c_size_t()
+        _native.check(native.mbg_material_constants(
+            b"cvr-rodr", C.byref(mat), 2e-17, 0, None, 0, C.byref(n)))
+        host = np.zeros(n.value)
+        devc = np.zeros(n.value)
+        for arr, on in ((host, 0), (devc, 1)):
+            _native.check(native.mbg_material_constants(
+                b"cvr-rodr", C.byref(mat), 2e-17, on,
+                arr.ctypes.data_as(T.PD), arr.size, C.byref(n)))
+        L = _native.material_layout("cvr-rodr", N)
+        # the kernel inputs agree to rounding (Q may differ by plane
+        # orientation only if the arithmetic differs; it does not here)
+        np.testing.assert_allclose(devc[:L["stage"]], host[:L["stage"]],
+                                   rtol=1e-9, atol=1e-9 * np.abs(host).max())
+
+
+def test_errors_reported_like_reference(native):
+    from mbsolve_gb300 import solvergpu
+    # gap between regions: "region not found" (solver_cpu_fdtd.tpp:119-125)
+    qm = mb.qm_desc_2lvl(1e24, 2 * mb.PI * 2e14, 6.24e-11, 1e10, 1e10)
+    m = mb.material("gap", qm)
+    mb.material.add_to_library(m)
+    dev = mb.device("gap")
+    dev.add_region(mb.region("a", m, 0, 1e-6))
+    dev.add_region(mb.region("b", m, 2e-6, 3e-6))
+    sce = mb.scenario("s", 64, 1e-15, mb.ic_density_const(
+        mb.qm_operator([1, 0])), mb.ic_field_const(0.0))
+    with pytest.raises(RuntimeError, match="region not found"):
+        solvergpu.solver_gpu_fdtd(dev, sce, "gpu-fdtd-2lvl-cvr-rodr-fp32")
+    # level count mismatch
+    dev2, sce2 = setups.sit_2lvl(64, 10)
+    with pytest.raises(RuntimeError, match="does not match"):
+        solvergpu.solver_gpu_fdtd(dev2, sce2, "gpu-fdtd-3lvl-cvr-rodr-fp32")

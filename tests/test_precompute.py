@@ -1,0 +1,114 @@
+"""The engine's FP64 precompute (host instantiation of the code the GPU
+runs) against the oracle: one step of the plane-basis update equals one
+step of the reference's dense Rodrigues update; the Cayley constants are
+the closed forms. CPU only."""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+import scipy.linalg
+
+from mbsolve_gb300 import capi_types as T
+from mbsolve_gb300 import lib as mb
+from mbsolve_gb300 import setups
+
+
+def _constants(native, algo, mat, dt):
+    from mbsolve_gb300 import _native
+    n = C.c_size_t()
+    _native.check(native.mbg_material_constants(algo.encode(), C.byref(mat),
+                                                dt, 0, None, 0, C.byref(n)))
+    out = np.zeros(n.value)
+    _native.check(native.mbg_material_constants(
+        algo.encode(), C.byref(mat), dt, 0, out.ctypes.data_as(T.PD),
+        out.size, C.byref(n)))
+    return out
+
+
+@pytest.mark.parametrize("N,seed", [(2, 0), (3, 1), (4, 2), (5, 3), (6, 4)])
+def test_plane_basis_step_equals_dense_rodrigues(native, N, seed):
+    from mbsolve_gb300 import _native
+    from oracle import oracle as O
+    dev, sce = setups.random_nlvl(N=N, num_gridpoints=16, num_timesteps=10,
+                                  seed=seed)
+    b = mb.to_pod(dev, sce)
+    mat = b.device.materials[0]
+    dt = 2.5e-17
+    L = _native.material_layout("cvr-rodr", N)
+    V = L["V"]
+    c = _constants(native, "cvr-rodr", mat, dt)
+    Q = c[L["Q"]:L["Q"] + V * V].reshape(V, V)
+    np.testing.assert_allclose(Q.T @ Q, np.eye(V), atol=1e-12)
+    Bd = c[L["Bd"]:L["Bd"] + V * V].reshape(V, V)
+    cc = c[L["c"]:L["c"] + V]
+    g = c[L["g"]:L["g"] + V]
+    th = c[L["thdt"]:L["thdt"] + V // 2]
+    p0 = c[L["p0"]]
+    rng = np.random.default_rng(seed)
+    for e in (0.0, 3e7, -8e8):
+        o = O.rodr_constants(mat.qm.contents, dt, e * dt)
+        d = rng.normal(size=V) * 0.3
+        # reference update (algo_lindblad_cvr_rodr.hpp:234-268)
+        d1 = o["A1"] @ (d + o["d_in"]) - o["d_in"]
+        d2 = o["A2"] @ d1
+        dr = o["A1"] @ (d2 + o["d_in"]) - o["d_in"]
+        pr = o["M_CP"] * o["v"] @ (o["M"] @ dr + o["d_eq"])
+        # plane-basis update
+        z = Q.T @ (d + o["d_in"])
+        w = z + Bd @ z - cc
+        for k in range(V // 2):
+            phi = th[k] * e
+            a, bb = w[2 * k], w[2 * k + 1]
+            w[2 * k] = math.cos(phi) * a - math.sin(phi) * bb
+            w[2 * k + 1] = math.sin(phi) * a + math.cos(phi) * bb
+        w = w + cc
+        z2 = w + Bd @ w
+        dg = Q @ z2 - o["d_in"]
+        pg = p0 + g @ z2
+        np.testing.assert_allclose(dg, dr, rtol=0, atol=1e-12)
+        assert abs(pg - pr) <= 1e-10 * max(1.0, abs(pr)) + 1e-6 * abs(
+            o["M_CP"] * o["v"] @ (np.abs(o["M"]) @ np.abs(dr)))
+    # observables: inversion is d[N(N-1)]
+    d = rng.normal(size=V)
+    z = Q.T @ (d + o["d_in"])
+    inv = c[L["inv"]:L["inv"] + V] @ z + c[L["inv_c"]]
+    assert abs(inv - d[N * (N - 1)]) < 1e-12
+
+
+def test_cayley_constants(native):
+    from mbsolve_gb300 import _native
+    dev, sce = setups.random_nlvl(N=3, num_gridpoints=16, num_timesteps=10,
+                                  seed=7)
+    b = mb.to_pod(dev, sce)
+    mat = b.device.materials[0]
+    dt = 2.5e-17
+    L = _native.material_layout("reg-cayley", 3)
+    c = _constants(native, "reg-cayley", mat, dt)
+    qm = mb.material.get_from_library(dev.get_used_materials()[0]).get_qm()
+    S = np.array(qm.get_relaxation_superop().get_scattering_rates())
+    dD1 = c[L["dD1"]:L["dD1"] + 9].reshape(3, 3)
+    np.testing.assert_allclose(dD1, scipy.linalg.expm(S * dt / 2) - np.eye(3),
+                               rtol=1e-9, atol=1e-20)
+    deph = qm.get_relaxation_superop().get_dephasing_rates()
+    np.testing.assert_allclose(c[L["dD2"]:L["dD2"] + 3],
+                               np.expm1(np.array(deph) * dt / 2), rtol=1e-12)
+    kappa = dt / (2 * mb.HBAR)
+    hd = qm.get_hamiltonian().get_main_diagonal()
+    np.testing.assert_allclose(c[L["kH0"]:L["kH0"] + 3], np.array(hd) * kappa,
+                               rtol=1e-14)
+
+
+def test_level_mismatch_is_rejected(native):
+    from mbsolve_gb300 import _native
+    dev, sce = setups.random_nlvl(N=3, num_gridpoints=16, num_timesteps=10)
+    b = mb.to_pod(dev, sce)
+    mat = b.device.materials[0]
+    n = C.c_size_t()
+    # the engine derives N from the material; a 3-level material asked for
+    # as Cayley works, a wrong relaxation kind is rejected
+    mat.qm.contents.relax_kind = T.MBG_RELAX_NONE
+    rc = native.mbg_material_constants(b"reg-cayley", C.byref(mat), 1e-17, 0,
+                                       None, 0, C.byref(n))
+    assert rc == T.MBG_ERR_INVALID_ARGUMENT
+    assert b"Unsupported superoperator" in native.mbg_last_error()
