@@ -363,7 +363,6 @@ int mbg_material_constants(
             MBG_CK(cudaMalloc((void**) &dout, stride * sizeof(double)));
             MBG_CK(cudaMalloc((void**) &dcode, sizeof(int)));
             MBG_CK(cudaMemcpy(din, &in, sizeof(in), cudaMemcpyHostToDevice));
-            if (N >= 5) MBG_CK(cudaDeviceSetLimit(cudaLimitStackSize, 16384));
             mbg::launch_precompute(din, 1, kind, N, ws, ws_n, dout, stride, dcode, 0);
             MBG_CK(cudaGetLastError());
             MBG_CK(cudaMemcpy(res.data(), dout, stride * sizeof(double), cudaMemcpyDeviceToHost));

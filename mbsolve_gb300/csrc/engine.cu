@@ -725,8 +725,6 @@ private:
             mc64_.alloc(nm * mstride_);
             MBG_CK(cudaMemcpyAsync(din.p, mins.data(), mins.size() * sizeof(pre::mat_in),
                                    cudaMemcpyHostToDevice, stream_));
-            if (kind_.algo == ALGO_CVR && N >= 5)
-                MBG_CK(cudaDeviceSetLimit(cudaLimitStackSize, 16384));
             precompute_kernel<<<(unsigned) ((mins.size() + 63) / 64), 64, 0, stream_>>>(
                 din.p, (int) mins.size(), kind_.algo, N, ws.p, ws_stride, mc64_.p, mstride_, codes.p);
             MBG_CK(cudaGetLastError());
