@@ -1,0 +1,491 @@
+#!/usr/bin/env python
+"""Benchmark of the batched Maxwell-Bloch time loop on GB300.
+
+Workload (the metric's batched configuration): 4,096 independent 2-level
+runs in one ensemble, lengths uniform in 2,048-32,768 grid points, pulse
+area uniform in 0.5-4 pi, detuning uniform in +-5 %, T2 log-uniform in
+0.1-10 ps, 50,000 time steps each, FP32 bulk arithmetic with the FP64
+precompute; seeded synthetic parameters (numpy PCG64, seed 0 + rank).
+
+One bench step = one chunk of S time steps of every run (S = 50,000 //
+(warmup + steps), at most 2,500), so warm-up and timed steps together stay
+inside each run's 50,000 steps. The state (1.7 GB FP32) is far larger than
+L2 (129 MB); no flush is needed between steps.
+
+Also measured: the plain FP64 GPU path on the plain workload (16,384
+points, 100,000 steps), FP32 error against FP64 (on that workload and on a
+sample of ensemble runs), the kernel roofline, an end-to-end time through
+the C-ABI with host buffers, and the FP64 CPU oracle on the host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("cell-updates/s: batched FP32 vs plain FP64 on one GB300 at "
+          "stated E-field error")
+WORKLOAD = ("batched 2-level ensemble: 4,096 runs, 2,048-32,768 points, "
+            "area 0.5-4 pi, detuning +-5 %, T2 0.1-10 ps, 50,000 steps, "
+            "probe E at the output facet every step")
+# algorithmic bytes per cell-update, one pass, unblocked: E, H, P_t and the
+# 3 density reals read once and written once, 4 bytes each
+BYTES_PER_CELL_UPDATE_FP32 = 2 * 4 * (3 + 3)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--runs", type=int, default=4096)
+    p.add_argument("--run-steps", type=int, default=50000)
+    p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--no-cpu", action="store_true",
+                   help="skip the CPU-baseline sample")
+    p.add_argument("--no-extras", action="store_true",
+                   help="only the headline measurement")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------ helpers
+
+class Dist:
+    """torchrun ranks: barrier and max over ranks (NCCL on GPUs). The data
+    path has no collective: every rank owns its own runs."""
+
+    def __init__(self, n):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if torch.cuda.is_available():
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x):
+        if not self.pg:
+            return x
+        import torch
+        dev = "cuda" if torch.cuda.is_available() else "cpu"
+        t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if not self.pg:
+            return x
+        import torch
+        dev = "cuda" if torch.cuda.is_available() else "cpu"
+        t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def device_sync():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+    except Exception:
+        pass
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu),
+                 "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded),
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(cells, depth):
+    """DRAM bytes per launch of the tile kernel from the committed ncu
+    summary (captured on a smaller ensemble and scaled by cells when the
+    depth matches), or None."""
+    path = os.path.join(ROOT, "profiles", "tile_kernel_fp32_2lvl_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        if int(d.get("depth", -1)) != int(depth):
+            return None
+        return float(d["dram_bytes_per_launch"]) * cells / float(d["cells"])
+    except Exception:
+        return None
+
+
+# --------------------------------------------------------- CPU baseline
+
+def cpu_sample(seed, target_s=12.0, threads=None):
+    """The FP64 oracle (the reference's plain solver restated) on the host
+    cores, over the first runs of the ensemble for a bounded number of
+    steps; returns (cell-updates/s, description, threads)."""
+    from mbsolve_gb300 import lib as mb
+    from mbsolve_gb300 import setups
+    from oracle import oracle as O
+    threads = threads or os.cpu_count() or 1
+    runs, params = setups.ensemble_2lvl(num_runs=8, seed=seed)
+    # calibrate on the first run
+    dev, sce = runs[0]
+    o = O.OracleRun("cvr-rodr", 2, mb.to_pod(dev, sce))
+    t = time.perf_counter()
+    o.run(threads=threads, max_steps=100)
+    rate = sce.get_num_gridpoints() * 100 / (time.perf_counter() - t)
+    del o
+    total_cells = sum(s.get_num_gridpoints() for _, s in runs)
+    steps = int(max(50, min(50000, target_s * rate / total_cells)))
+    cu = 0
+    t0 = time.perf_counter()
+    for dev, sce in runs:
+        o = O.OracleRun("cvr-rodr", 2, mb.to_pod(dev, sce))
+        o.run(threads=threads, max_steps=steps)
+        cu += sce.get_num_gridpoints() * steps
+    dt = time.perf_counter() - t0
+    desc = ("first 8 runs of the ensemble (%d points), %d steps each, FP64 "
+            "oracle restating solver_cpu_fdtd<2, cvr_rodr>, OpenMP over "
+            "points" % (total_cells, steps))
+    return cu / dt, desc, threads, cu, dt
+
+
+def run_reference_arm(args, dist):
+    """--impl reference: the CPU implementation of the path (the oracle
+    restatement; the reference's own build needs its source tree, absent
+    here) on this machine's host cores, same metric and config."""
+    if dist.rank != 0:
+        return
+    from mbsolve_gb300 import lib as mb
+    from mbsolve_gb300 import setups
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    runs, _ = setups.ensemble_2lvl(num_runs=args.runs, seed=args.seed)
+    sample = runs[:4]
+    steps_per = 200
+    times = []
+    cu_total = 0
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        cu = 0
+        for dev, sce in sample:
+            o = O.OracleRun("cvr-rodr", 2, mb.to_pod(dev, sce))
+            o.run(threads=threads, max_steps=steps_per)
+            cu += sce.get_num_gridpoints() * steps_per
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt)
+            cu_total += cu
+    value = cu_total / sum(times)
+    desc = ("4 runs of the ensemble x %d steps per bench step, FP64 oracle "
+            "(C++ restatement of solver_cpu_fdtd<2, cvr_rodr>) on %d host "
+            "threads" % (steps_per, threads))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value,
+        "unit": "cell-updates/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "sample": desc},
+        "cpu_baseline": {"value": value, "unit": "cell-updates/s",
+                         "cores": threads, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": "cell-updates/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------- our arm
+
+def run_ours(args, dist):
+    import numpy as np
+    from mbsolve_gb300 import lib as mb
+    from mbsolve_gb300 import setups, ensemble, solvergpu
+
+    seed = args.seed + dist.rank
+    S = max(1, min(2500, args.run_steps // (args.warmup + args.steps)))
+    runs, params = setups.ensemble_2lvl(num_runs=args.runs,
+                                        num_timesteps=args.run_steps,
+                                        seed=seed)
+    ens = ensemble.ensemble("gpu-fdtd-2lvl-cvr-rodr-fp32", runs)
+    info = ens.info()
+    cells = info["cells"]
+    for _ in range(args.warmup):
+        ens.advance(S)
+    device_sync()
+    sampler = ClockSampler(dist.local)
+    sampler.start()
+    time.sleep(0.4)
+    ens.set_timing(True)
+    ens.kernel_time(reset=True)
+    l0 = ens.launches()
+    dist.barrier()
+    device_sync()
+    ens.region_begin()
+    for _ in range(args.steps):
+        ens.advance(S)
+    ms = ens.region_end()
+    device_sync()
+    dist.barrier()
+    launches = ens.launches() - l0
+    k_launches, k_ms = ens.kernel_time(reset=True)
+    ens.set_timing(False)
+    clocks = sampler.stop()
+    ms_max = dist.max(ms)
+    cu_rank = float(cells) * S * args.steps
+    cu_all = dist.sum(cu_rank)
+    value = cu_all / (ms_max * 1e-3)
+    status = ens.status()
+
+    # roofline of the dominant kernel (the FP32 2-level tile kernel)
+    hbm, peak_kind = peaks()
+    depth = info["depth"]
+    t_launch = k_ms * 1e-3 / max(1, k_launches)
+    alg_bytes = BYTES_PER_CELL_UPDATE_FP32 * cells * depth
+    achieved = alg_bytes / t_launch / 1e9
+    # state moved once per launch: the unavoidable bytes with blocking
+    blocked_bytes = BYTES_PER_CELL_UPDATE_FP32 * cells
+    traffic = ncu_traffic(cells, depth)
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+        "frac": achieved / hbm, "traffic": traffic,
+        "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+        "kernel": "cvr_step_kernel<float, V=3, C=%d, NT=%d>" % (
+            info["cells_per_thread"], info["threads"]),
+        "algorithmic_bytes_per_cell_update": BYTES_PER_CELL_UPDATE_FP32,
+        "cell_updates_per_launch": cells * depth,
+        "temporal_depth": depth,
+        "avg_launch_ms": t_launch * 1e3,
+        "state_bytes_per_launch": blocked_bytes,
+        "state_gbs": blocked_bytes / t_launch / 1e9,
+        "state_frac": blocked_bytes / t_launch / 1e9 / hbm,
+        "dram_gbs": (traffic / t_launch / 1e9) if traffic else None,
+        "note": "achieved counts 48 B per cell-update (one unblocked pass) x "
+                "cells x depth per launch; with temporal blocking the state "
+                "crosses HBM once per launch (state_gbs), so achieved may "
+                "exceed the copy peak",
+    }
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-updates/s",
+        "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded PCG64, seed %d + rank)" % args.seed,
+        "config": {
+            "workload": WORKLOAD, "runs_per_gpu": args.runs,
+            "cells_per_gpu": cells, "steps_per_run": args.run_steps,
+            "time_steps_per_bench_step": S,
+            "tuning": {k: info[k] for k in ("cells_per_thread", "threads",
+                                            "depth", "launches_per_graph")},
+            "tiles": info["tiles"],
+            "l2": "state %.2f GB > L2 129 MB; no flush between steps" % (
+                cells * 24 / 1e9),
+            "parallelism": "replicas: each GPU its own %d runs" % args.runs,
+        },
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "clocks": clocks,
+        "device_status": status,
+    }
+    del ens
+
+    if dist.rank == 0 and not args.no_extras:
+        # ---- plain FP64 GPU path and FP32 error on the plain workload
+        extras = {}
+        res = {}
+        for prec in ("fp64", "fp32"):
+            mb.material.clear_library()
+            dev, sce = setups.sit_2lvl(16384, 100000)
+            s = solvergpu.solver_gpu_fdtd(dev, sce,
+                                          "gpu-fdtd-2lvl-cvr-rodr-" + prec)
+            device_sync()
+            t0 = time.perf_counter()
+            s.run()
+            device_sync()
+            dt = time.perf_counter() - t0
+            res[prec] = (s.get_results()[0].as_array().ravel(), dt)
+        plain = 16384 * 100000 / res["fp64"][1]
+        e32 = np.linalg.norm(res["fp32"][0] - res["fp64"][0]) / \
+            np.linalg.norm(res["fp64"][0])
+        extras["plain_fp64"] = {
+            "value": plain, "unit": "cell-updates/s",
+            "workload": "plain 2-level: 16,384 points, 100,000 steps, FP64 "
+                        "(gpu-fdtd-2lvl-cvr-rodr-fp64, run() wall time)"}
+        extras["ratio_vs_plain_fp64"] = value / plain
+        err = {"plain_fp32_vs_fp64_rel_l2": e32}
+        # FP64 GPU vs the FP64 CPU oracle on the plain workload
+        try:
+            from oracle import oracle as O
+            mb.material.clear_library()
+            dev, sce = setups.sit_2lvl(16384, 100000)
+            o = O.OracleRun("cvr-rodr", 2, mb.to_pod(dev, sce))
+            o.run(threads=os.cpu_count())
+            ref = o.results()[0][0].ravel()
+            err["plain_fp64_vs_oracle_rel_l2"] = float(
+                np.linalg.norm(res["fp64"][0] - ref) / np.linalg.norm(ref))
+            err["plain_fp32_vs_oracle_rel_l2"] = float(
+                np.linalg.norm(res["fp32"][0] - ref) / np.linalg.norm(ref))
+        except Exception as e:
+            err["oracle"] = "not run: %s" % e
+        # ensemble sample: FP32 vs FP64 over all 50,000 steps
+        mb.material.clear_library()
+        sample = 32
+        idx = list(range(sample))
+        out = {}
+        for prec in ("fp32", "fp64"):
+            mb.material.clear_library()
+            rs, _ = setups.ensemble_2lvl(num_runs=args.runs,
+                                         num_timesteps=args.run_steps,
+                                         seed=seed)
+            e = ensemble.ensemble("gpu-fdtd-2lvl-cvr-rodr-" + prec,
+                                  [rs[i] for i in idx])
+            e.run()
+            out[prec] = e.probe_rows(0, 0, args.run_steps)
+            del e
+        num = np.linalg.norm(out["fp32"] - out["fp64"])
+        den = np.linalg.norm(out["fp64"])
+        err["ensemble_sample_fp32_vs_fp64_rel_l2"] = float(num / den)
+        per = [float(np.linalg.norm(out["fp32"][i] - out["fp64"][i]) /
+                     np.linalg.norm(out["fp64"][i]))
+               for i in range(sample) if np.linalg.norm(out["fp64"][i]) > 0]
+        err["ensemble_sample_max_run_rel_l2"] = max(per) if per else None
+        err["ensemble_sample"] = "first %d runs, full %d steps" % (
+            sample, args.run_steps)
+        extras["error"] = err
+
+        # ---- end to end through the C-ABI with host buffers
+        mb.material.clear_library()
+        device_sync()
+        t0 = time.perf_counter()
+        rs, _ = setups.ensemble_2lvl(num_runs=args.runs,
+                                     num_timesteps=args.run_steps, seed=seed)
+        e = ensemble.ensemble("gpu-fdtd-2lvl-cvr-rodr-fp32", rs)
+        h2d = e.pod_bytes()
+        d2h = 0
+        for k in range(args.steps):
+            e.advance(S)
+            rows = e.probe_rows(0, k * S, S)
+            d2h += args.runs * S * 4
+        device_sync()
+        dt = time.perf_counter() - t0
+        extras["e2e"] = {
+            "value": float(cells) * S * args.steps / dt,
+            "unit": "cell-updates/s",
+            "h2d_bytes_per_step": int(h2d / args.steps),
+            "d2h_bytes_per_step": int(d2h / args.steps),
+            "includes": "host scenario description -> create (set-up, FP64 "
+                        "precompute, initial state) + per step advance and "
+                        "D2H of the step's probe samples",
+        }
+        del e
+        line.update(extras)
+    elif dist.rank == 0:
+        line["e2e"] = None
+
+    if dist.rank == 0 and not args.no_cpu:
+        v, desc, th, cu, dt = cpu_sample(seed)
+        line["cpu_baseline"] = {"value": v, "unit": "cell-updates/s",
+                                "cores": th, "kind": "port", "sample": desc,
+                                "seconds": dt}
+    if dist.rank == 0:
+        print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    dist = Dist(args.gpus)
+    try:
+        if args.impl == "reference":
+            run_reference_arm(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -308,6 +308,13 @@ int mbg_ensemble_kernel_time(
     uint64_t* launches,
     double* milliseconds,
     int reset);
+/* Device time of a region of work on the ensemble's stream: begin = 1
+ * records a start event, begin = 0 records a stop event, waits for it and
+ * writes the milliseconds between the two. */
+int mbg_ensemble_stream_time(mbg_ensemble* e, int begin, double* milliseconds);
+/* Kernels this library launched on the ensemble's stream so far (time-step
+ * kernels and the small clock/gather kernels around them). */
+int mbg_ensemble_launches(const mbg_ensemble* e, uint64_t* launches);
 /* Status flags raised on the device (bit 0: non-finite probe value). */
 int mbg_ensemble_status(mbg_ensemble* e, uint32_t* flags);
 void mbg_ensemble_destroy(mbg_ensemble* e);

@@ -72,6 +72,9 @@ def load():
     L.mbg_ensemble_kernel_time.argtypes = [C.c_void_p, P(C.c_uint64),
                                            P(C.c_double), C.c_int]
     L.mbg_ensemble_status.argtypes = [C.c_void_p, P(C.c_uint32)]
+    L.mbg_ensemble_launches.argtypes = [C.c_void_p, P(C.c_uint64)]
+    L.mbg_ensemble_stream_time.argtypes = [C.c_void_p, C.c_int,
+                                           P(C.c_double)]
     L.mbg_ensemble_destroy.argtypes = [C.c_void_p]
     L.mbg_material_constants.argtypes = [C.c_char_p, P(T.mbg_material),
                                          C.c_double, C.c_int, T.PD,

@@ -306,6 +306,23 @@ int mbg_ensemble_kernel_time(mbg_ensemble* e, uint64_t* launches, double* ms, in
     });
 }
 
+int mbg_ensemble_stream_time(mbg_ensemble* e, int begin, double* ms)
+{
+    return guarded([&] {
+        if (!e || (!begin && !ms)) throw mbg::invalid_argument("null argument");
+        double t = e->eng->stream_time(begin != 0);
+        if (!begin) *ms = t;
+    });
+}
+
+int mbg_ensemble_launches(const mbg_ensemble* e, uint64_t* launches)
+{
+    return guarded([&] {
+        if (!e || !launches) throw mbg::invalid_argument("null argument");
+        *launches = e->eng->launches();
+    });
+}
+
 int mbg_ensemble_status(mbg_ensemble* e, uint32_t* flags)
 {
     return guarded([&] {

@@ -562,6 +562,7 @@ public:
         if (!steps) return;
         step_set_kernel<<<1, 1, 0, stream_>>>(step_.p, (unsigned long long) steps_done_);
         MBG_CK(cudaGetLastError());
+        launches_ += 1;
         const uint64_t depth = tune_.depth;
         uint64_t full = steps / depth;
         const uint64_t rem = steps % depth;
@@ -619,6 +620,7 @@ public:
                                cudaMemcpyHostToDevice, stream_));
         gather_probe_kernel<T><<<1024, 256, 0, stream_>>>(scratch_.p, doffs.p, nr, row0, nrows, tmp.p);
         MBG_CK(cudaGetLastError());
+        launches_ += 1;
         std::vector<T> h((size_t) nr * nrows);
         MBG_CK(cudaMemcpyAsync(h.data(), tmp.p, h.size() * sizeof(T), cudaMemcpyDeviceToHost, stream_));
         MBG_CK(cudaStreamSynchronize(stream_));
@@ -659,6 +661,31 @@ private:
     size_t ev_used_ = 0, ev_read_ = 0;
     double acc_ms_ = 0;
     uint64_t acc_launches_ = 0;
+    uint64_t launches_ = 0;  // every kernel launched by advance()/copies
+
+    cudaEvent_t region_[2] = { nullptr, nullptr };
+
+public:
+    uint64_t launches() const override { return launches_; }
+
+    double stream_time(bool begin) override
+    {
+        if (!region_[0]) {
+            MBG_CK(cudaEventCreate(&region_[0]));
+            MBG_CK(cudaEventCreate(&region_[1]));
+        }
+        if (begin) {
+            MBG_CK(cudaEventRecord(region_[0], stream_));
+            return 0.0;
+        }
+        MBG_CK(cudaEventRecord(region_[1], stream_));
+        MBG_CK(cudaEventSynchronize(region_[1]));
+        float ms = 0;
+        MBG_CK(cudaEventElapsedTime(&ms, region_[0], region_[1]));
+        return ms;
+    }
+
+private:
 
     void setup()
     {
@@ -996,6 +1023,7 @@ private:
         if (timing_) MBG_CK(cudaEventRecord(ev->b, stream_));
         step_bump_kernel<<<1, 1, 0, stream_>>>(step_.p, (unsigned long long) count * nsub);
         MBG_CK(cudaGetLastError());
+        launches_ += count + 1;
     }
 
     void replay_graph()
@@ -1023,6 +1051,7 @@ private:
             MBG_CK(cudaEventRecord(ev->a, stream_));
         }
         MBG_CK(cudaGraphLaunch(graph_exec_[cur_], stream_));
+        launches_ += L + 1;
         if (timing_) MBG_CK(cudaEventRecord(ev->b, stream_));
         if (L % 2) cur_ = 1 - cur_;
     }

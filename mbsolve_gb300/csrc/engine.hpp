@@ -90,6 +90,9 @@ public:
     virtual void set_timing(bool on) = 0;
     virtual void kernel_time(uint64_t* launches, double* ms, bool reset) = 0;
     virtual uint32_t status() = 0;
+    virtual uint64_t launches() const = 0;
+    // begin: record a start event; else record a stop event, wait, return ms
+    virtual double stream_time(bool begin) = 0;
 };
 
 std::unique_ptr<engine> make_engine(

@@ -104,6 +104,27 @@ class ensemble:
             self._h, C.byref(n), C.byref(ms), int(reset)))
         return n.value, ms.value
 
+    def region_begin(self):
+        """Start a CUDA-event timed region on the ensemble's stream."""
+        _native.check(self._L.mbg_ensemble_stream_time(self._h, 1, None))
+
+    def region_end(self):
+        """End the region; returns its device time in milliseconds."""
+        ms = C.c_double()
+        _native.check(self._L.mbg_ensemble_stream_time(self._h, 0,
+                                                       C.byref(ms)))
+        return ms.value
+
+    def launches(self):
+        """Kernel launches issued so far on this ensemble's stream."""
+        n = C.c_uint64()
+        _native.check(self._L.mbg_ensemble_launches(self._h, C.byref(n)))
+        return n.value
+
+    def pod_bytes(self):
+        """Bytes of host description data handed to the engine."""
+        return sum(C.sizeof(o) for b in self._bundles for o in b.keep)
+
     def status(self):
         f = C.c_uint32()
         _native.check(self._L.mbg_ensemble_status(self._h, C.byref(f)))

@@ -65,6 +65,29 @@ def golden_cases():
     return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
 
 
+def plane_basis_step(c, L, d, d_in, e):
+    """One update of the engine's plane-basis form (numpy, FP64) from a
+    constant block `c` with layout `L`: returns (d', P) for coherence
+    vector d, field e and the material's d_in."""
+    import math
+    V = L["V"]
+    Q = c[L["Q"]:L["Q"] + V * V].reshape(V, V)
+    Bd = c[L["Bd"]:L["Bd"] + V * V].reshape(V, V)
+    cc = c[L["c"]:L["c"] + V]
+    g = c[L["g"]:L["g"] + V]
+    th = c[L["thdt"]:L["thdt"] + V // 2]
+    z = Q.T @ (d + d_in)
+    w = z + Bd @ z - cc
+    for k in range(V // 2):
+        phi = th[k] * e
+        a, b = w[2 * k], w[2 * k + 1]
+        w[2 * k] = math.cos(phi) * a - math.sin(phi) * b
+        w[2 * k + 1] = math.sin(phi) * a + math.cos(phi) * b
+    w = w + cc
+    z2 = w + Bd @ w
+    return Q @ z2 - d_in, c[L["p0"]] + g @ z2
+
+
 def tuning(C_=0, NT=0, depth=0, graph=0):
     t = T.mbg_tuning()
     t.cells_per_thread = C_

@@ -148,10 +148,18 @@ def test_device_precompute_equals_host(native):
                 b"cvr-rodr", C.byref(mat), 2e-17, on,
                 arr.ctypes.data_as(T.PD), arr.size, C.byref(n)))
         L = _native.material_layout("cvr-rodr", N)
-        # the kernel inputs agree to rounding (Q may differ by plane
-        # orientation only if the arithmetic differs; it does not here)
-        np.testing.assert_allclose(devc[:L["stage"]], host[:L["stage"]],
-                                   rtol=1e-9, atol=1e-9 * np.abs(host).max())
+        # the plane basis is not unique (degenerate planes, null space), so
+        # compare what it computes: one update from the same state
+        from oracle import oracle as O
+        d_in = O.rodr_constants(mat.qm.contents, 2e-17, 0.0)["d_in"]
+        rng = np.random.default_rng(N)
+        for e in (0.0, 2e8, -7e8):
+            d = rng.normal(size=L["V"]) * 0.3
+            dh, ph = helpers.plane_basis_step(host, L, d, d_in, e)
+            dd, pd = helpers.plane_basis_step(devc, L, d, d_in, e)
+            np.testing.assert_allclose(dd, dh, rtol=0, atol=1e-12)
+            # P ~ n mu omega ~ 1e10 A/m^2 for these media
+            assert abs(pd - ph) <= 1e-8 * max(abs(ph), 1e10)
 
 
 def test_errors_reported_like_reference(native):
