@@ -408,7 +408,9 @@ size_t mbg_material_layout(const char* algo, uint32_t N, char* buf, size_t len)
         mbg::pre::cvr_layout L = mbg::pre::make_cvr_layout((int) N);
         s << "V=" << L.V << "\nKP=" << L.KP << "\na=" << L.a << "\nb=" << L.b << "\ncH=" << L.cH
           << "\ngamma=" << L.gam << "\nhas_qm=" << L.has_qm << "\np0=" << L.p0 << "\nnplanes=" << L.nplanes
-          << "\nBd=" << L.Bd << "\nc=" << L.c << "\ng=" << L.g << "\nthdt=" << L.thdt << "\nz0=" << L.z0
+          << "\nBd=" << L.Bd << "\nBdl=" << L.Bdl << "\nk=" << L.k << "\ng=" << L.g << "\nthdt=" << L.thdt
+          << "\nu0=" << L.z0 << "\nbdx=" << mbg::pre::FD_BDX << "\nbdx_lo=" << mbg::pre::FD_BDX_LO
+          << "\ncH_lo=" << mbg::pre::FD_C_LO << "\nbG=" << mbg::pre::FD_G
           << "\ninv=" << L.inv << "\ninv_c=" << L.inv_c << "\npop=" << L.pop << "\npop_c=" << L.pop_c
           << "\nQ=" << L.Q << "\nstage=" << L.stage << "\nstride=" << L.stride;
     } else if (a == "reg-cayley") {

@@ -354,6 +354,8 @@ __global__ void init_kernel(
     T* H,
     T* P,
     T* D,
+    T* El,  // low parts of the double-float fields (FP32), or null
+    T* Hl,
     uint64_t plane,
     uint32_t* status)
 {
@@ -371,15 +373,25 @@ __global__ void init_kernel(
                 }
             if (m < 0) atomicOr(status, STATUS_REGION);
             mat[g] = m;
-            E[g] = (T) (d.e_kind == MBG_FIELD_IC_VALUES ? e_vals[d.e_off + l] : d.e_val);
-            H[g] = (T) (d.h_kind == MBG_FIELD_IC_VALUES ? h_vals[d.h_off + l] : d.h_val);
+            const double e0 = d.e_kind == MBG_FIELD_IC_VALUES ? e_vals[d.e_off + l] : d.e_val;
+            const double h0 = d.h_kind == MBG_FIELD_IC_VALUES ? h_vals[d.h_off + l] : d.h_val;
+            E[g] = (T) e0;
+            H[g] = (T) h0;
+            if (El) El[g] = (T) (e0 - (double) E[g]);
+            if (Hl) Hl[g] = (T) (h0 - (double) H[g]);
             P[g] = T(0);
             if (m < 0 || planes == 0) continue;
             const double* cb = mc64 + (size_t) m * mstride;
             const bool qm = cb[4] != 0.0;
             if (algo == ALGO_CVR) {
                 const pre::cvr_layout L = pre::make_cvr_layout(N);
-                for (int v = 0; v < planes; v++) D[(uint64_t) v * plane + g] = qm ? (T) cb[L.z0 + v] : T(0);
+                const int V = L.V;
+                for (int v = 0; v < V; v++) {
+                    const double u0 = qm ? cb[L.z0 + v] : 0.0;
+                    D[(uint64_t) v * plane + g] = (T) u0;
+                    // FP32: the low word of the float pair
+                    if (planes == 2 * V) D[(uint64_t) (V + v) * plane + g] = (T) (u0 - (double) (T) u0);
+                }
             } else {
                 const pre::cay_layout L = pre::make_cay_layout(N);
                 for (int v = 0; v < planes; v++) D[(uint64_t) v * plane + g] = qm ? (T) cb[L.rho0 + v] : T(0);
@@ -395,9 +407,9 @@ struct srcgen_desc {
     uint64_t table_offset;
 };
 
-// Source values get_value(j dt) (source.hpp:94-106, 190-194, 256-260).
-template<typename T>
-__global__ void source_kernel(const srcgen_desc* s, uint32_t n, T* tab)
+// Source values get_value(j dt) (source.hpp:94-106, 190-194, 256-260),
+// kept in FP64 for both precisions.
+__global__ void source_kernel(const srcgen_desc* s, uint32_t n, double* tab)
 {
     for (uint32_t k = blockIdx.y; k < n; k += gridDim.y) {
         const srcgen_desc d = s[k];
@@ -411,7 +423,7 @@ __global__ void source_kernel(const srcgen_desc* s, uint32_t n, T* tab)
                 v = d.ampl *
                     (exp(-(t - d.phase) * (t - d.phase) / (d.beta_or_tau * d.beta_or_tau)) *
                      sin(2 * PI * d.freq * t));
-            tab[d.table_offset + j] = (T) v;
+            tab[d.table_offset + j] = v;
         }
     }
 }
@@ -501,7 +513,10 @@ public:
     engine_t(const solver_kind& k, std::vector<run_setup>&& runs, const mbg_tuning* t)
       : kind_(k), runs_(std::move(runs))
     {
-        planes_ = (k.algo == ALGO_CVR) ? k.N * k.N - 1 : (k.algo == ALGO_CAYLEY) ? k.N * k.N : 0;
+        // FP32 coherence vectors are float pairs: V high then V low planes
+        planes_ = (k.algo == ALGO_CVR) ? (k.N * k.N - 1) * (DF ? 2 : 1)
+            : (k.algo == ALGO_CAYLEY)  ? k.N * k.N
+                                       : 0;
         MBG_CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
         setup();
         choose_tuning(t);
@@ -642,8 +657,11 @@ private:
     int mstride_ = 0, mstage_ = 0;
     int cur_ = 0;  // buffer holding the current state
     dbuf<T> E_[2], H_[2], P_[2], D_[2];
+    dbuf<T> El_[2], Hl_[2];  // FP32: low parts of the double-float fields
+    static constexpr bool DF = sizeof(T) == 4;
     dbuf<int32_t> mat_;
-    dbuf<T> mc_, stab_, scratch_;
+    dbuf<T> mc_, scratch_;
+    dbuf<double> stab_;
     dbuf<double> mc64_;
     dbuf<run_desc> runs_dev_;
     dbuf<src_desc> srcs_;
@@ -710,6 +728,12 @@ private:
             if (planes_) {
                 D_[b].alloc(n_total_ * planes_);
                 MBG_CK(cudaMemsetAsync(D_[b].p, 0, n_total_ * planes_ * sizeof(T), stream_));
+            }
+            if (DF) {
+                El_[b].alloc(n_total_);
+                Hl_[b].alloc(n_total_);
+                MBG_CK(cudaMemsetAsync(El_[b].p, 0, n_total_ * sizeof(T), stream_));
+                MBG_CK(cudaMemsetAsync(Hl_[b].p, 0, n_total_ * sizeof(T), stream_));
             }
         }
         mat_.alloc(n_total_);
@@ -815,7 +839,8 @@ private:
             dim3 grid(256, std::min<uint32_t>(nr, 65535));
             init_kernel<T><<<grid, 256, 0, stream_>>>(
                 dids.p, nr, dregs.p, dev_e.p, dev_h.p, mc64_.p, mstride_, kind_.algo, N, planes_,
-                mat_.p, E_[0].p, H_[0].p, P_[0].p, planes_ ? D_[0].p : nullptr, n_total_, status_.p);
+                mat_.p, E_[0].p, H_[0].p, P_[0].p, planes_ ? D_[0].p : nullptr, DF ? El_[0].p : nullptr,
+                DF ? Hl_[0].p : nullptr, n_total_, status_.p);
             MBG_CK(cudaGetLastError());
             MBG_CK(cudaStreamSynchronize(stream_));
         }
@@ -874,7 +899,7 @@ private:
             MBG_CK(cudaMemcpyAsync(dg.p, gens.data(), gens.size() * sizeof(srcgen_desc),
                                    cudaMemcpyHostToDevice, stream_));
             dim3 grid(64, std::min<size_t>(gens.size(), 65535));
-            source_kernel<T><<<grid, 256, 0, stream_>>>(dg.p, (uint32_t) gens.size(), stab_.p);
+            source_kernel<<<grid, 256, 0, stream_>>>(dg.p, (uint32_t) gens.size(), stab_.p);
             MBG_CK(cudaGetLastError());
             MBG_CK(cudaStreamSynchronize(stream_));
         }
@@ -890,9 +915,9 @@ private:
             for (uint32_t r = 0; r < nr; r++)
                 for (const auto& s : runs_[r].sources) {
                     if (!s.on_grid || s.shape != MBG_SHAPE_TABLE) continue;
-                    cast_kernel<T><<<64, 256, 0, stream_>>>(dt.p + pos, stab_.p + table_dst[src_i],
-                                                            runs_[r].n_t);
-                    MBG_CK(cudaGetLastError());
+                    MBG_CK(cudaMemcpyAsync(stab_.p + table_dst[src_i], dt.p + pos,
+                                           runs_[r].n_t * sizeof(double), cudaMemcpyDeviceToDevice,
+                                           stream_));
                     pos += runs_[r].n_t;
                     src_i++;
                 }
@@ -972,6 +997,10 @@ private:
         p.Hout = H_[out].p;
         p.Pout = P_[out].p;
         p.Dout = planes_ ? D_[out].p : nullptr;
+        p.Elin = DF ? El_[in].p : nullptr;
+        p.Hlin = DF ? Hl_[in].p : nullptr;
+        p.Elout = DF ? El_[out].p : nullptr;
+        p.Hlout = DF ? Hl_[out].p : nullptr;
         p.plane = n_total_;
         p.mat = mat_.p;
         p.mc = mc_.p;

@@ -6,16 +6,10 @@
 
 namespace mbg {
 
-template<typename T, int V, int C, int NT>
-void launch_cvr(const kparams<T>& p, unsigned grid, size_t smem, cudaStream_t s)
+template<typename T, int ALGO, int LEV, int C, int NT>
+void launch_step(const kparams<T>& p, unsigned grid, size_t smem, cudaStream_t s)
 {
-    cvr_step_kernel<T, V, C, NT><<<grid, NT, smem, s>>>(p);
-}
-
-template<typename T, int N, int C, int NT>
-void launch_cay(const kparams<T>& p, unsigned grid, size_t smem, cudaStream_t s)
-{
-    cayley_step_kernel<T, N, C, NT><<<grid, NT, smem, s>>>(p);
+    step_kernel<T, ALGO, LEV, C, NT><<<grid, NT, smem, s>>>(p);
 }
 
 }  // namespace mbg
@@ -24,10 +18,10 @@ void launch_cay(const kparams<T>& p, unsigned grid, size_t smem, cudaStream_t s)
 #define MBG_CAT(a, b) MBG_CAT2(a, b)
 #define MBG_REG_CVR(T, LEV, C, NT)                                            \
     static const bool MBG_CAT(mbg_reg_, __LINE__) = ::mbg::register_kernel<T>( \
-        ::mbg::ALGO_CVR, LEV, C, NT, &::mbg::launch_cvr<T, (LEV) * (LEV) - 1, C, NT>);
+        ::mbg::ALGO_CVR, LEV, C, NT, &::mbg::launch_step<T, 1, LEV, C, NT>);
 #define MBG_REG_NOOP(T, C, NT)                                                \
     static const bool MBG_CAT(mbg_reg_, __LINE__) = ::mbg::register_kernel<T>( \
-        ::mbg::ALGO_NOOP, 0, C, NT, &::mbg::launch_cvr<T, 0, C, NT>);
+        ::mbg::ALGO_NOOP, 0, C, NT, &::mbg::launch_step<T, 0, 0, C, NT>);
 #define MBG_REG_CAY(T, LEV, C, NT)                                            \
     static const bool MBG_CAT(mbg_reg_, __LINE__) = ::mbg::register_kernel<T>( \
-        ::mbg::ALGO_CAYLEY, LEV, C, NT, &::mbg::launch_cay<T, LEV, C, NT>);
+        ::mbg::ALGO_CAYLEY, LEV, C, NT, &::mbg::launch_step<T, 2, LEV, C, NT>);

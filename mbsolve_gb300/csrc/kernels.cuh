@@ -15,9 +15,16 @@
 // Neighbour values cross thread boundaries by warp shuffles and cross warp
 // boundaries through shared memory (two barriers per step). Garbage from
 // the tile edges moves one point per step, so after `nsub <= halo` steps
-// the output range is exact. Points outside the run carry zero
-// coefficients and zero state; the reference's index rules (no H update at
-// i = 0, H[N] = 0) give them no influence on the run.
+// the output range is exact. Points outside the run keep zero state and
+// are never updated; the reference's index rules (no H update at i = 0,
+// H[N] = 0) give them no influence on the run.
+//
+// FP32 kernels keep E and H as unevaluated sums hi + lo of two floats and
+// update them with error-free transformations (TwoSum; TwoProd by fma):
+// the spatial differences of FP32 fields lose about log2(points per
+// wavelength) bits, which over 1e5 steps dominates the error; with the
+// double-float fields the FP32 result tracks the FP64 one closely while
+// density, polarisation and all matrix work stay in FP32.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -33,10 +40,14 @@ struct kparams {
     const T* Hin;
     const T* Pin;
     const T* Din;  // density planes, `plane` apart
+    const T* Elin; // FP32 only: low parts of E and H (double-float fields)
+    const T* Hlin;
     T* Eout;
     T* Hout;
     T* Pout;
     T* Dout;
+    T* Elout;
+    T* Hlout;
     uint64_t plane;
     const int32_t* mat;  // global material index per point (-1: none)
     const T* mc;         // material constant blocks
@@ -45,7 +56,7 @@ struct kparams {
     const tile_desc* tiles;
     const run_desc* runs;
     const src_desc* srcs;
-    const T* stab;       // source value tables
+    const double* stab;  // source value tables (FP64)
     const rec_desc* recs;
     T* scratch;
     const unsigned long long* step_base;  // device step counter
@@ -169,31 +180,33 @@ __device__ __forceinline__ void store_cells(
 template<typename T, int V>
 struct cvr_coef {
     static constexpr int KP = V / 2;
-    static constexpr int oBd = 8;
-    static constexpr int oc = 8 + V * V;
-    static constexpr int og = oc + V;
+    static constexpr int oBd = pre::FDTD_END;
+    static constexpr int oBdl = oBd + V * V;
+    static constexpr int ok = oBdl + V * V;
+    static constexpr int og = ok + V;
     static constexpr int oth = og + V;
     const T* base;
     __device__ __forceinline__ T Bd(int i, int j) const { return base[oBd + i * V + j]; }
-    __device__ __forceinline__ T c(int i) const { return base[oc + i]; }
+    __device__ __forceinline__ T Bdl(int i, int j) const { return base[oBdl + i * V + j]; }
+    __device__ __forceinline__ T k(int i) const { return base[ok + i]; }
     __device__ __forceinline__ T g(int i) const { return base[og + i]; }
     __device__ __forceinline__ T th(int k) const { return base[oth + k]; }
     __device__ __forceinline__ T p0() const { return base[5]; }
 };
 
 // Coherence-vector update in the plane basis (see precompute.cuh):
-// w = z + Bd z - c; rotate each plane by theta_k dt e; z = (w + c) + Bd (w + c);
-// P = p0 + g . z.
+// w = u + (Bd u + k); rotate each plane by theta_k dt e; u = w + (Bd w + k);
+// P = p0 + g . u.
 template<typename T, int V, class CF>
-__device__ __forceinline__ void cvr_update(T (&z)[V], T e, T& pout, const CF& cf)
+__device__ __forceinline__ void cvr_update(T (&u)[V], T e, T& pout, const CF& cf)
 {
     T w[V];
 #pragma unroll
     for (int i = 0; i < V; i++) {
-        T s = z[i] - cf.c(i);
+        T s = cf.k(i);
 #pragma unroll
-        for (int j = 0; j < V; j++) s = fma(cf.Bd(i, j), z[j], s);
-        w[i] = s;
+        for (int j = 0; j < V; j++) s = fma(cf.Bd(i, j), u[j], s);
+        w[i] = u[i] + s;
     }
 #pragma unroll
     for (int k = 0; k < V / 2; k++) {
@@ -203,16 +216,71 @@ __device__ __forceinline__ void cvr_update(T (&z)[V], T e, T& pout, const CF& cf
         w[2 * k] = a - fma(s2, a, sn * b);
         w[2 * k + 1] = b + fma(sn, a, -s2 * b);
     }
-#pragma unroll
-    for (int i = 0; i < V; i++) w[i] += cf.c(i);
     T pp = cf.p0();
 #pragma unroll
     for (int i = 0; i < V; i++) {
-        T s = w[i];
+        T s = cf.k(i);
 #pragma unroll
         for (int j = 0; j < V; j++) s = fma(cf.Bd(i, j), w[j], s);
-        z[i] = s;
-        pp = fma(cf.g(i), s, pp);
+        u[i] = w[i] + s;
+        pp = fma(cf.g(i), u[i], pp);
+    }
+    pout = pp;
+}
+
+// hi + lo <- hi + lo + d (TwoSum, then renormalised)
+__device__ __forceinline__ void df_acc(float& h, float& l, float d, float extra_lo)
+{
+    const float s = h + d;
+    const float bv = s - h;
+    const float err = (h - (s - bv)) + (d - bv);
+    const float e2 = l + err + extra_lo;
+    h = s + e2;
+    l = e2 - (h - s);
+}
+
+// The same update in FP32 with u = uh + ul: the corrections are computed in
+// FP32 from the high words and accumulated error-free; the low words take
+// the rounding errors and the Bdl contribution.
+template<int V, class CF>
+__device__ __forceinline__ void cvr_update_df(float (&uh)[V], float (&ul)[V], float e, float& pout, const CF& cf)
+{
+    float wh[V], wl[V];
+#pragma unroll
+    for (int i = 0; i < V; i++) {
+        float c = cf.k(i), cl = 0.0f;
+#pragma unroll
+        for (int j = 0; j < V; j++) {
+            c = fmaf(cf.Bd(i, j), uh[j], c);
+            cl = fmaf(cf.Bdl(i, j), uh[j], cl);
+        }
+        wh[i] = uh[i];
+        wl[i] = ul[i];
+        df_acc(wh[i], wl[i], c, cl);
+    }
+#pragma unroll
+    for (int k = 0; k < V / 2; k++) {
+        float sn, s2;
+        rot_coeffs<float>(cf.th(k) * e, sn, s2);
+        const float a = wh[2 * k], b = wh[2 * k + 1];
+        const float da = -fmaf(s2, a, sn * b);
+        const float db = fmaf(sn, a, -s2 * b);
+        df_acc(wh[2 * k], wl[2 * k], da, 0.0f);
+        df_acc(wh[2 * k + 1], wl[2 * k + 1], db, 0.0f);
+    }
+    float pp = cf.p0();
+#pragma unroll
+    for (int i = 0; i < V; i++) {
+        float c = cf.k(i), cl = 0.0f;
+#pragma unroll
+        for (int j = 0; j < V; j++) {
+            c = fmaf(cf.Bd(i, j), wh[j], c);
+            cl = fmaf(cf.Bdl(i, j), wh[j], cl);
+        }
+        uh[i] = wh[i];
+        ul[i] = wl[i];
+        df_acc(uh[i], ul[i], c, cl);
+        pp = fmaf(cf.g(i), uh[i], fmaf(cf.g(i), ul[i], pp));
     }
     pout = pp;
 }
@@ -278,175 +346,70 @@ __device__ __forceinline__ void store_record(
     if (!isfinite(v)) atomicOr(p.status, STATUS_NONFINITE);
 }
 
-// --------------------------------------------------- CVR / Maxwell kernel
-//
-// V = N^2 - 1 density reals per point (V = 0: Maxwell only, the noop
-// algorithm of algo_lindblad_noop.hpp).
-template<typename T, int V, int C, int NT>
-__global__ void __launch_bounds__(NT) cvr_step_kernel(const kparams<T> p)
+
+// ------------------------------------------------------- field updates
+
+struct fcoef {
+    float a, bh, bl, g, ch, cl;
+};
+
+__device__ __forceinline__ fcoef load_fcoef(const float* cb)
 {
-    constexpr int NW = NT / 32;
-    constexpr int VV = V > 0 ? V : 1;
-    constexpr int NLEV = V == 3 ? 2 : V == 8 ? 3 : V == 15 ? 4 : V == 24 ? 5 : V == 35 ? 6 : 0;
-    __shared__ T sh_h[NW];
-    __shared__ T sh_e[NW];
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sh_coef = reinterpret_cast<T*>(smem_raw);
+    return fcoef{ cb[pre::FD_A], cb[pre::FD_BDX], cb[pre::FD_BDX_LO],
+                  cb[pre::FD_G], cb[pre::FD_C], cb[pre::FD_C_LO] };
+}
 
-    const tile_desc td = p.tiles[blockIdx.x];
-    const run_desc rd = p.runs[td.run];
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int64_t l0 = (int64_t) td.out_start - (int64_t) p.halo + (int64_t) threadIdx.x * C;
-    const int64_t g0 = (int64_t) rd.offset + l0;
-    const int64_t nx = rd.n_x;
-    const uint64_t step0 = *p.step_base + (uint64_t) p.launch_idx * p.depth;
-    int nsteps = 0;
-    if (step0 < rd.n_t) nsteps = (int) min((uint64_t) p.nsub, (uint64_t) rd.n_t - step0);
+// hi + lo <- a (hi + lo) + (b/dx) (dh + dl) - b Gamma P, error-free except
+// for the final renormalisation
+__device__ __forceinline__ void df_e_update(
+    float& eh,
+    float& el,
+    float dh,
+    float dl,
+    float pt,
+    const fcoef& f)
+{
+    const float ph = f.bh * dh;
+    const float pe = fmaf(f.bh, dh, -ph);
+    const float pl = pe + fmaf(f.bh, dl, f.bl * dh) - f.g * pt;
+    float xh = eh, xl = el;
+    if (f.a != 1.0f) {
+        xh = f.a * eh;
+        xl = fmaf(f.a, eh, -xh) + f.a * el;
+    }
+    const float s = xh + ph;
+    const float bv = s - xh;
+    const float err = (xh - (s - bv)) + (ph - bv);
+    const float e2 = err + (xl + pl);
+    eh = s + e2;
+    el = e2 - (eh - s);
+}
 
-    T E[C], H[C], P[C];
-    T Z[C][VV];
-    int32_t M[C];
-    load_cells<T, C>(E, p.Ein, g0);
-    load_cells<T, C>(H, p.Hin, g0);
-    load_cells<T, C>(P, p.Pin, g0);
-    if constexpr (V > 0) {
-#pragma unroll
-        for (int v = 0; v < V; v++) {
-            T tmp[C];
-            load_cells<T, C>(tmp, p.Din + (uint64_t) v * p.plane, g0);
-#pragma unroll
-            for (int j = 0; j < C; j++) Z[j][v] = tmp[j];
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < C; j++) {
-        const int64_t l = l0 + j;
-        const bool valid = (l >= 0) && (l < nx);
-        M[j] = valid ? __ldg(p.mat + g0 + j) : -1;
-        if (!valid) {
-            E[j] = H[j] = P[j] = T(0);
-#pragma unroll
-            for (int v = 0; v < VV; v++) Z[j][v] = T(0);
-        }
-    }
-    const bool uniform = td.uniform_mat >= 0;
-    if (uniform) {
-        const T* src = p.mc + (uint64_t) td.uniform_mat * p.mstride;
-        for (int i = threadIdx.x; i < (int) p.mstage; i += NT) sh_coef[i] = src[i];
-    }
-    __syncthreads();
-    const T dxi = (T) rd.dx_inv;
+// hi + lo <- hi + lo + c (dh + dl)
+__device__ __forceinline__ void df_h_update(float& hh, float& hl, float dh, float dl, const fcoef& f)
+{
+    const float ph = f.ch * dh;
+    const float pe = fmaf(f.ch, dh, -ph);
+    const float pl = pe + fmaf(f.ch, dl, f.cl * dh);
+    const float s = hh + ph;
+    const float bv = s - hh;
+    const float err = (hh - (s - bv)) + (ph - bv);
+    const float e2 = err + (hl + pl);
+    hh = s + e2;
+    hl = e2 - (hh - s);
+}
 
-    for (int m = 0; m < nsteps; m++) {
-        const uint64_t n = step0 + (uint64_t) m;
-        // ---- E update: needs H of the right neighbour
-        if (lane == 0) sh_h[warp] = H[0];
-        __syncthreads();
-        T hr = __shfl_down_sync(0xffffffffu, H[0], 1);
-        if (lane == 31) hr = (warp + 1 < NW) ? sh_h[warp + 1] : T(0);
-#pragma unroll
-        for (int j = 0; j < C; j++) {
-            const T hn = (j + 1 < C) ? H[j + 1] : hr;
-            T a, b, gam;
-            if (uniform) {
-                a = sh_coef[0];
-                b = sh_coef[1];
-                gam = sh_coef[3];
-            } else if (M[j] >= 0) {
-                const T* cb = p.mc + (uint64_t) M[j] * p.mstride;
-                a = cb[0];
-                b = cb[1];
-                gam = cb[3];
-            } else {
-                a = b = gam = T(0);
-            }
-            const bool valid = M[j] >= 0;
-            T en = a * E[j] + b * (-gam * P[j] + (hn - H[j]) * dxi);
-            E[j] = valid ? en : T(0);
-        }
-        // ---- sources (after E, before H)
-        for (uint32_t s = rd.src_begin; s < rd.src_end; s++) {
-            const src_desc sd = p.srcs[s];
-            const int64_t jj = (int64_t) sd.x_idx - l0;
-            if (jj >= 0 && jj < C) {
-                const T val = p.stab[sd.table_offset + n];
-#pragma unroll
-                for (int j = 0; j < C; j++)
-                    if (j == jj && M[j] >= 0) E[j] = (sd.type == 0) ? val : E[j] + val;
-            }
-        }
-        // ---- H update: needs E of the left neighbour
-        if (lane == 31) sh_e[warp] = E[C - 1];
-        __syncthreads();
-        T el = __shfl_up_sync(0xffffffffu, E[C - 1], 1);
-        if (lane == 0) el = (warp > 0) ? sh_e[warp - 1] : T(0);
-#pragma unroll
-        for (int j = 0; j < C; j++) {
-            const int64_t l = l0 + j;
-            const T ep = (j > 0) ? E[j - 1] : el;
-            if (l >= 1 && l < nx) {
-                T cH = uniform ? sh_coef[2] : p.mc[(uint64_t) M[j] * p.mstride + 2];
-                H[j] += cH * (E[j] - ep);
-            } else if (l == 0) {
-                H[j] = T(0);
-            }
-        }
-        // ---- density update and polarisation current
-        if constexpr (V > 0) {
-            if (uniform) {
-                if (sh_coef[4] != T(0)) {
-                    cvr_coef<T, V> cf{ sh_coef };
-#pragma unroll
-                    for (int j = 0; j < C; j++)
-                        if (M[j] >= 0) cvr_update<T, V>(Z[j], E[j], P[j], cf);
-                }
-            } else {
-#pragma unroll
-                for (int j = 0; j < C; j++) {
-                    if (M[j] < 0) continue;
-                    const T* cb = p.mc + (uint64_t) M[j] * p.mstride;
-                    if (cb[4] == T(0)) continue;
-                    cvr_coef<T, V> cf{ cb };
-                    cvr_update<T, V>(Z[j], E[j], P[j], cf);
-                }
-            }
-        }
-        // ---- recording
-        if (p.record) {
-            for (uint32_t r = rd.rec_begin; r < rd.rec_end; r++) {
-                const rec_desc rc = p.recs[r];
-                if (!hasto_record(rc.ratio, n)) continue;
-                const int64_t lo = max((int64_t) rc.pos, (int64_t) td.out_start);
-                const int64_t hi = min((int64_t) rc.pos + rc.cols,
-                                       (int64_t) td.out_start + td.out_len);
-                if (l0 + C <= lo || l0 >= hi) continue;
-#pragma unroll
-                for (int j = 0; j < C; j++) {
-                    const int64_t l = l0 + j;
-                    if (l < lo || l >= hi) continue;
-                    const T* cb = p.mc + (uint64_t) (M[j] >= 0 ? M[j] : 0) * p.mstride;
-                    T v = cvr_record_value<T, V>(rc, E[j], H[j], P[j], Z[j], cb, NLEV);
-                    store_record<T>(p, rc, n, l, v);
-                }
-            }
-        }
-    }
-
-    // ---- write back the output range
-    const int64_t lo = td.out_start, hi = (int64_t) td.out_start + td.out_len;
-    store_cells<T, C>(E, p.Eout, g0, l0, lo, hi);
-    store_cells<T, C>(H, p.Hout, g0, l0, lo, hi);
-    store_cells<T, C>(P, p.Pout, g0, l0, lo, hi);
-    if constexpr (V > 0) {
-#pragma unroll
-        for (int v = 0; v < V; v++) {
-            T tmp[C];
-#pragma unroll
-            for (int j = 0; j < C; j++) tmp[j] = Z[j][v];
-            store_cells<T, C>(tmp, p.Dout + (uint64_t) v * p.plane, g0, l0, lo, hi);
-        }
-    }
+// hi + lo += v (v in FP64)
+__device__ __forceinline__ void df_add(float& hh, float& hl, double v)
+{
+    const float vh = (float) v;
+    const float vl = (float) (v - (double) vh);
+    const float s = hh + vh;
+    const float bv = s - hh;
+    const float err = (hh - (s - bv)) + (vh - bv);
+    const float e2 = err + (hl + vl);
+    hh = s + e2;
+    hl = e2 - (hh - s);
 }
 
 // ---------------------------------------------------- Cayley kernel
@@ -702,20 +665,201 @@ __device__ __forceinline__ void cayley_update(T (&rho)[N * N], T e, T& pout, con
     pout = acc;
 }
 
-template<typename T, int N, int C, int NT>
-__global__ void __launch_bounds__(NT) cayley_step_kernel(const kparams<T> p)
+// ------------------------------------------------------- the tile kernel
+//
+// ALGO 0: Maxwell only (algo_lindblad_noop.hpp), 1: coherence vector /
+// Rodrigues, 2: Cayley. D density reals per point: 0, N^2 - 1, N^2.
+
+template<int ALGO, int LEV>
+struct density_len {
+    static constexpr int value = ALGO == 1 ? LEV * LEV - 1 : ALGO == 2 ? LEV * LEV : 0;
+};
+
+template<typename T, int ALGO, int LEV, int C, int NT, bool UNIFORM>
+__device__ __forceinline__ void tile_steps(
+    const kparams<T>& p,
+    const tile_desc& td,
+    const run_desc& rd,
+    int64_t l0,
+    int nsteps,
+    uint64_t step0,
+    T (&E)[C],
+    T (&El)[C],
+    T (&H)[C],
+    T (&Hl)[C],
+    T (&P)[C],
+    T (&R)[C][density_len<ALGO, LEV>::value > 0 ? density_len<ALGO, LEV>::value : 1],
+    T (&Rl)[C][density_len<ALGO, LEV>::value > 0 ? density_len<ALGO, LEV>::value : 1],
+    const int32_t (&M)[C],
+    const T* sh_coef,
+    T* sh_a,
+    T* sh_al,
+    T* sh_b,
+    T* sh_bl)
 {
+    constexpr bool DF = sizeof(T) == 4;
+    constexpr int D = density_len<ALGO, LEV>::value;
     constexpr int NW = NT / 32;
-    constexpr int D = N * N;
-    __shared__ T sh_h[NW];
-    __shared__ T sh_e[NW];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int64_t nx = rd.n_x;
+    const T dxi = (T) rd.dx_inv;
+    // coefficient block of point j
+    auto block = [&](int j) -> const T* {
+        return UNIFORM ? sh_coef : p.mc + (uint64_t) (M[j] >= 0 ? M[j] : 0) * p.mstride;
+    };
+    fcoef fu;
+    if constexpr (DF && UNIFORM) fu = load_fcoef(sh_coef);
+
+    for (int m = 0; m < nsteps; m++) {
+        const uint64_t n = step0 + (uint64_t) m;
+        // ---- E: needs H (hi, lo) of the right neighbour
+        if (lane == 0) {
+            sh_a[warp] = H[0];
+            if constexpr (DF) sh_al[warp] = Hl[0];
+        }
+        __syncthreads();
+        T hr = __shfl_down_sync(0xffffffffu, H[0], 1);
+        T hrl = DF ? __shfl_down_sync(0xffffffffu, Hl[0], 1) : T(0);
+        if (lane == 31) {
+            hr = (warp + 1 < NW) ? sh_a[warp + 1] : T(0);
+            if constexpr (DF) hrl = (warp + 1 < NW) ? sh_al[warp + 1] : T(0);
+        }
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            if (M[j] < 0) continue;
+            const T hn = (j + 1 < C) ? H[j + 1] : hr;
+            if constexpr (DF) {
+                const T hnl = (j + 1 < C) ? Hl[j + 1] : hrl;
+                const fcoef f = UNIFORM ? fu : load_fcoef(block(j));
+                df_e_update(E[j], El[j], hn - H[j], hnl - Hl[j], P[j], f);
+            } else {
+                const T* cb = block(j);
+                E[j] = cb[pre::FD_A] * E[j] +
+                    cb[pre::FD_B] * (-cb[pre::FD_GAMMA] * P[j] + (hn - H[j]) * dxi);
+            }
+        }
+        // ---- sources, after E and before H (solver_cpu_fdtd.tpp:245-255)
+        for (uint32_t s = rd.src_begin; s < rd.src_end; s++) {
+            const src_desc sd = p.srcs[s];
+            const int64_t jj = (int64_t) sd.x_idx - l0;
+            if (jj >= 0 && jj < C) {
+                const double v = p.stab[sd.table_offset + n];
+#pragma unroll
+                for (int j = 0; j < C; j++) {
+                    if (j != jj || M[j] < 0) continue;
+                    if (sd.type == 0) {
+                        E[j] = (T) v;
+                        if constexpr (DF) El[j] = (T) (v - (double) E[j]);
+                    } else {
+                        if constexpr (DF)
+                            df_add(E[j], El[j], v);
+                        else
+                            E[j] += (T) v;
+                    }
+                }
+            }
+        }
+        // ---- H: needs E (hi, lo) of the left neighbour
+        if (lane == 31) {
+            sh_b[warp] = E[C - 1];
+            if constexpr (DF) sh_bl[warp] = El[C - 1];
+        }
+        __syncthreads();
+        T el = __shfl_up_sync(0xffffffffu, E[C - 1], 1);
+        T ell = DF ? __shfl_up_sync(0xffffffffu, El[C - 1], 1) : T(0);
+        if (lane == 0) {
+            el = (warp > 0) ? sh_b[warp - 1] : T(0);
+            if constexpr (DF) ell = (warp > 0) ? sh_bl[warp - 1] : T(0);
+        }
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            const int64_t l = l0 + j;
+            if (l >= 1 && l < nx) {
+                const T ep = (j > 0) ? E[j - 1] : el;
+                if constexpr (DF) {
+                    const T epl = (j > 0) ? El[j - 1] : ell;
+                    const fcoef f = UNIFORM ? fu : load_fcoef(block(j));
+                    df_h_update(H[j], Hl[j], E[j] - ep, El[j] - epl, f);
+                } else {
+                    H[j] += block(j)[pre::FD_C] * (E[j] - ep);
+                }
+            } else if (l == 0) {
+                H[j] = T(0);
+                if constexpr (DF) Hl[j] = T(0);
+            }
+        }
+        // ---- density matrix and polarisation current at every point
+        if constexpr (D > 0) {
+#pragma unroll
+            for (int j = 0; j < C; j++) {
+                if (M[j] < 0) continue;
+                const T* cb = block(j);
+                if (cb[pre::FD_HAS_QM] == T(0)) continue;
+                const T e = DF ? E[j] + El[j] : E[j];
+                if constexpr (ALGO == 1) {
+                    cvr_coef<T, D> cf{ cb };
+                    if constexpr (DF)
+                        cvr_update_df<D>(R[j], Rl[j], e, P[j], cf);
+                    else
+                        cvr_update<T, D>(R[j], e, P[j], cf);
+                } else {
+                    cayley_update<T, LEV>(R[j], e, P[j], cb);
+                }
+            }
+        }
+        // ---- recording (solver_cpu_fdtd.tpp:288-325)
+        if (p.record) {
+            for (uint32_t r = rd.rec_begin; r < rd.rec_end; r++) {
+                const rec_desc rc = p.recs[r];
+                if (!hasto_record(rc.ratio, n)) continue;
+                const int64_t lo = max((int64_t) rc.pos, (int64_t) td.out_start);
+                const int64_t hi = min((int64_t) rc.pos + rc.cols, (int64_t) td.out_start + td.out_len);
+                if (l0 + C <= lo || l0 >= hi) continue;
+#pragma unroll
+                for (int j = 0; j < C; j++) {
+                    const int64_t l = l0 + j;
+                    if (l < lo || l >= hi) continue;
+                    const T ev = DF ? E[j] + El[j] : E[j];
+                    const T hv = DF ? H[j] + Hl[j] : H[j];
+                    T v = T(0);
+                    if constexpr (ALGO == 2) {
+                        switch (rc.type) {
+                        case 0: v = ev; break;
+                        case 1: v = P[j]; break;
+                        case 2: v = hv; break;
+                        case 4: v = R[j][1] - R[j][0]; break;
+                        case 3:
+                            if (rc.row_idx == rc.col_idx && rc.row_idx < (uint32_t) LEV) v = R[j][rc.row_idx];
+                            break;
+                        }
+                    } else {
+                        constexpr int DDv = D > 0 ? D : 1;
+                        T u[DDv];
+#pragma unroll
+                        for (int q = 0; q < DDv; q++) u[q] = DF ? R[j][q] + Rl[j][q] : R[j][q];
+                        v = cvr_record_value<T, D>(rc, ev, hv, P[j], u, block(j), LEV);
+                    }
+                    store_record<T>(p, rc, n, l, v);
+                }
+            }
+        }
+    }
+}
+
+template<typename T, int ALGO, int LEV, int C, int NT>
+__global__ void __launch_bounds__(NT) step_kernel(const kparams<T> p)
+{
+    constexpr bool DF = sizeof(T) == 4;
+    constexpr int D = density_len<ALGO, LEV>::value;
+    constexpr int DD = D > 0 ? D : 1;
+    constexpr int NW = NT / 32;
+    __shared__ T sh_a[NW], sh_al[NW], sh_b[NW], sh_bl[NW];
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sh_coef = reinterpret_cast<T*>(smem_raw);
 
     const tile_desc td = p.tiles[blockIdx.x];
     const run_desc rd = p.runs[td.run];
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
     const int64_t l0 = (int64_t) td.out_start - (int64_t) p.halo + (int64_t) threadIdx.x * C;
     const int64_t g0 = (int64_t) rd.offset + l0;
     const int64_t nx = rd.n_x;
@@ -723,29 +867,47 @@ __global__ void __launch_bounds__(NT) cayley_step_kernel(const kparams<T> p)
     int nsteps = 0;
     if (step0 < rd.n_t) nsteps = (int) min((uint64_t) p.nsub, (uint64_t) rd.n_t - step0);
 
-    T E[C], H[C], Pc[C];
-    T R[C][D];
+    T E[C], El[C], H[C], Hl[C], P[C];
+    T R[C][DD];
+    T Rl[C][DD];  // FP32 coherence vector: low words
+    constexpr bool DFD = DF && ALGO == 1;
     int32_t M[C];
     load_cells<T, C>(E, p.Ein, g0);
     load_cells<T, C>(H, p.Hin, g0);
-    load_cells<T, C>(Pc, p.Pin, g0);
+    load_cells<T, C>(P, p.Pin, g0);
+    if constexpr (DF) {
+        load_cells<T, C>(El, p.Elin, g0);
+        load_cells<T, C>(Hl, p.Hlin, g0);
+    }
+    if constexpr (D > 0) {
 #pragma unroll
-    for (int v = 0; v < D; v++) {
-        T tmp[C];
-        load_cells<T, C>(tmp, p.Din + (uint64_t) v * p.plane, g0);
+        for (int v = 0; v < D; v++) {
+            T tmp[C];
+            load_cells<T, C>(tmp, p.Din + (uint64_t) v * p.plane, g0);
 #pragma unroll
-        for (int j = 0; j < C; j++) R[j][v] = tmp[j];
+            for (int j = 0; j < C; j++) R[j][v] = tmp[j];
+            if constexpr (DFD) {
+                load_cells<T, C>(tmp, p.Din + (uint64_t) (D + v) * p.plane, g0);
+#pragma unroll
+                for (int j = 0; j < C; j++) Rl[j][v] = tmp[j];
+            }
+        }
     }
 #pragma unroll
     for (int j = 0; j < C; j++) {
+        if constexpr (!DFD)
+#pragma unroll
+            for (int v = 0; v < DD; v++) Rl[j][v] = T(0);
         const int64_t l = l0 + j;
         const bool valid = (l >= 0) && (l < nx);
         M[j] = valid ? __ldg(p.mat + g0 + j) : -1;
         if (!valid) {
-            E[j] = H[j] = Pc[j] = T(0);
+            E[j] = H[j] = P[j] = T(0);
+            El[j] = Hl[j] = T(0);
 #pragma unroll
-            for (int v = 0; v < D; v++) R[j][v] = T(0);
+            for (int v = 0; v < DD; v++) R[j][v] = Rl[j][v] = T(0);
         }
+        if constexpr (!DF) El[j] = Hl[j] = T(0);
     }
     const bool uniform = td.uniform_mat >= 0;
     if (uniform) {
@@ -753,116 +915,60 @@ __global__ void __launch_bounds__(NT) cayley_step_kernel(const kparams<T> p)
         for (int i = threadIdx.x; i < (int) p.mstage; i += NT) sh_coef[i] = src[i];
     }
     __syncthreads();
-    const T dxi = (T) rd.dx_inv;
-    const pre::cay_layout L = pre::make_cay_layout(N);
 
-    for (int m = 0; m < nsteps; m++) {
-        const uint64_t n = step0 + (uint64_t) m;
-        if (lane == 0) sh_h[warp] = H[0];
-        __syncthreads();
-        T hr = __shfl_down_sync(0xffffffffu, H[0], 1);
-        if (lane == 31) hr = (warp + 1 < NW) ? sh_h[warp + 1] : T(0);
-#pragma unroll
-        for (int j = 0; j < C; j++) {
-            const T hn = (j + 1 < C) ? H[j + 1] : hr;
-            const T* cb = uniform ? sh_coef : p.mc + (uint64_t) (M[j] >= 0 ? M[j] : 0) * p.mstride;
-            const bool valid = M[j] >= 0;
-            T en = cb[0] * E[j] + cb[1] * (-cb[3] * Pc[j] + (hn - H[j]) * dxi);
-            E[j] = valid ? en : T(0);
-        }
-        for (uint32_t s = rd.src_begin; s < rd.src_end; s++) {
-            const src_desc sd = p.srcs[s];
-            const int64_t jj = (int64_t) sd.x_idx - l0;
-            if (jj >= 0 && jj < C) {
-                const T val = p.stab[sd.table_offset + n];
-#pragma unroll
-                for (int j = 0; j < C; j++)
-                    if (j == jj && M[j] >= 0) E[j] = (sd.type == 0) ? val : E[j] + val;
-            }
-        }
-        if (lane == 31) sh_e[warp] = E[C - 1];
-        __syncthreads();
-        T el = __shfl_up_sync(0xffffffffu, E[C - 1], 1);
-        if (lane == 0) el = (warp > 0) ? sh_e[warp - 1] : T(0);
-#pragma unroll
-        for (int j = 0; j < C; j++) {
-            const int64_t l = l0 + j;
-            const T ep = (j > 0) ? E[j - 1] : el;
-            if (l >= 1 && l < nx) {
-                const T* cb = uniform ? sh_coef : p.mc + (uint64_t) M[j] * p.mstride;
-                H[j] += cb[2] * (E[j] - ep);
-            } else if (l == 0) {
-                H[j] = T(0);
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < C; j++) {
-            if (M[j] < 0) continue;
-            const T* cb = uniform ? sh_coef : p.mc + (uint64_t) M[j] * p.mstride;
-            if (cb[4] == T(0)) continue;  // no qm: density stays zero
-            cayley_update<T, N>(R[j], E[j], Pc[j], cb);
-        }
-        if (p.record) {
-            for (uint32_t r = rd.rec_begin; r < rd.rec_end; r++) {
-                const rec_desc rc = p.recs[r];
-                if (!hasto_record(rc.ratio, n)) continue;
-                const int64_t lo = max((int64_t) rc.pos, (int64_t) td.out_start);
-                const int64_t hi = min((int64_t) rc.pos + rc.cols,
-                                       (int64_t) td.out_start + td.out_len);
-                if (l0 + C <= lo || l0 >= hi) continue;
-#pragma unroll
-                for (int j = 0; j < C; j++) {
-                    const int64_t l = l0 + j;
-                    if (l < lo || l >= hi) continue;
-                    T v = T(0);
-                    switch (rc.type) {
-                    case 0: v = E[j]; break;
-                    case 1: v = Pc[j]; break;
-                    case 2: v = H[j]; break;
-                    case 4: v = R[j][1] - R[j][0]; break;
-                    case 3:
-                        if (rc.row_idx == rc.col_idx && rc.row_idx < (uint32_t) N)
-                            v = R[j][rc.row_idx];
-                        break;
-                    }
-                    store_record<T>(p, rc, n, l, v);
-                }
-            }
-        }
-    }
-    // FP32: renormalise the trace to that of the initial density matrix, in
-    // FP64, once per launch (the exact propagators preserve the trace: the
-    // scattering matrix has zero column sums and U2 is unitary; this removes
-    // FP32 round-off drift)
-    if constexpr (sizeof(T) == 4) {
+    if (uniform)
+        tile_steps<T, ALGO, LEV, C, NT, true>(p, td, rd, l0, nsteps, step0, E, El, H, Hl, P, R, Rl, M,
+                                              sh_coef, sh_a, sh_al, sh_b, sh_bl);
+    else
+        tile_steps<T, ALGO, LEV, C, NT, false>(p, td, rd, l0, nsteps, step0, E, El, H, Hl, P, R, Rl, M,
+                                               sh_coef, sh_a, sh_al, sh_b, sh_bl);
+
+    // Cayley, FP32: renormalise the trace to that of the initial density
+    // matrix, in FP64, once per launch (the exact propagators preserve it:
+    // the scattering matrix has zero column sums and U2 is unitary; this
+    // removes FP32 round-off drift)
+    if constexpr (ALGO == 2 && DF) {
+        const pre::cay_layout L = pre::make_cay_layout(LEV);
 #pragma unroll
         for (int j = 0; j < C; j++) {
             if (M[j] < 0 || nsteps == 0) continue;
             const T* cb = uniform ? sh_coef : p.mc + (uint64_t) M[j] * p.mstride;
-            if (cb[4] == T(0)) continue;
+            if (cb[pre::FD_HAS_QM] == T(0)) continue;
             double tr = 0.0, target = 0.0;
 #pragma unroll
-            for (int i = 0; i < N; i++) {
+            for (int i = 0; i < LEV; i++) {
                 tr += (double) R[j][i];
                 target += (double) cb[L.rho0 + i];
             }
             if (tr != 0.0 && fabs(tr / target - 1.0) < 1e-3) {
                 const float s = (float) (target / tr);
 #pragma unroll
-                for (int v = 0; v < D; v++) R[j][v] *= s;
+                for (int v = 0; v < DD; v++) R[j][v] *= s;
             }
         }
     }
+
     const int64_t lo = td.out_start, hi = (int64_t) td.out_start + td.out_len;
     store_cells<T, C>(E, p.Eout, g0, l0, lo, hi);
     store_cells<T, C>(H, p.Hout, g0, l0, lo, hi);
-    store_cells<T, C>(Pc, p.Pout, g0, l0, lo, hi);
+    store_cells<T, C>(P, p.Pout, g0, l0, lo, hi);
+    if constexpr (DF) {
+        store_cells<T, C>(El, p.Elout, g0, l0, lo, hi);
+        store_cells<T, C>(Hl, p.Hlout, g0, l0, lo, hi);
+    }
+    if constexpr (D > 0) {
 #pragma unroll
-    for (int v = 0; v < D; v++) {
-        T tmp[C];
+        for (int v = 0; v < D; v++) {
+            T tmp[C];
 #pragma unroll
-        for (int j = 0; j < C; j++) tmp[j] = R[j][v];
-        store_cells<T, C>(tmp, p.Dout + (uint64_t) v * p.plane, g0, l0, lo, hi);
+            for (int j = 0; j < C; j++) tmp[j] = R[j][v];
+            store_cells<T, C>(tmp, p.Dout + (uint64_t) v * p.plane, g0, l0, lo, hi);
+            if constexpr (DFD) {
+#pragma unroll
+                for (int j = 0; j < C; j++) tmp[j] = Rl[j][v];
+                store_cells<T, C>(tmp, p.Dout + (uint64_t) (D + v) * p.plane, g0, l0, lo, hi);
+            }
+        }
     }
 }
 

@@ -9,16 +9,21 @@
 // coherence vector d by
 //     d1 = A1 (d + d_in) - d_in,  d2 = A2(e) d1,  d = A1 (d2 + d_in) - d_in
 // with A1 = exp(M dt/2) and A2(e) = exp(e dt U), U skew-symmetric, A2 built
-// from the real-Schur planes of U. Here the state is kept in the basis Q of
-// those planes: z = Q^T (d + d_in). Then
-//     z <- B (R(e) (B z - c) + c),  B = Q^T A1 Q,  c = Q^T d_in,
+// from the real-Schur planes of U. Here the state is the same vector in the
+// basis Q of those planes, u = Q^T d. With B = Q^T A1 Q = I + Bd,
+// F = A1 - I and the small constant k = Q^T F d_in (A1 d + F d_in is the
+// reference's first half step):
+//     w = u + (Bd u + k);  w <- R(e) w;  u = w + (Bd w + k)
 // where R(e) is block-diagonal with a 2x2 rotation by theta_k e dt per plane
 // and the identity on the null space of U: two V x V products and V/2 plane
 // rotations per point and step instead of forming A2. The polarisation
-// current p_t = M_CP v^T (M d + d_eq) becomes g^T z + p0 with
-// g = M_CP Q^T M^T v and p0 = M_CP v^T (d_eq - M d_in). B is stored as
-// B - I (computed from exp(X) - I directly), so that the FP32 kernels add a
-// small correction to an exact identity.
+// current p_t = M_CP v^T (M d + d_eq) becomes g^T u + p0 with
+// g = M_CP Q^T M^T v and p0 = M_CP v^T d_eq. Every stage adds a small
+// correction to a vector of norm about 1; Bd comes from exp(X) - I computed
+// directly. The FP32 kernels keep u as a float pair (hi + lo), add the
+// corrections with TwoSum and add Bdl = Bd - fl32(Bd) into the low word:
+// otherwise the FP32 rounding of Bd acts as a systematic shift of the
+// transition frequency.
 //
 // Planes of U: U is real skew-symmetric, so i U is complex Hermitian with
 // eigenvalues +-theta_k; an eigenvector a + i b for +theta gives the
@@ -75,11 +80,30 @@ MBG_HD cd cconj(cd a) { return cd{ a.re, -a.im }; }
 
 // ------------------------------------------------------------- layouts
 
+// Leading FDTD part of every material block (both algorithms):
+//   0 a, 1 b, 2 c, 3 Gamma       (common_fdtd.hpp:131-190)
+//   4 has_qm, 5 p0 (CVR), 6 nplanes (CVR), 7 unused
+//   8 b/dx, 9 b/dx - fl32(b/dx), 10 c - fl32(c), 11 b Gamma
+// Entries 8-11 serve the FP32 kernels, which keep E and H as unevaluated
+// sums of two floats and need the coefficients to the same accuracy.
+enum : int {
+    FD_A = 0,
+    FD_B = 1,
+    FD_C = 2,
+    FD_GAMMA = 3,
+    FD_HAS_QM = 4,
+    FD_BDX = 8,
+    FD_BDX_LO = 9,
+    FD_C_LO = 10,
+    FD_G = 11,
+    FDTD_END = 12
+};
+
 // Constant block of one material for the coherence-vector kernels.
 struct cvr_layout {
     int N, V, KP;
     int a, b, cH, gam, has_qm, p0, nplanes;
-    int Bd, c, g, thdt, z0, inv, inv_c, pop, pop_c;
+    int Bd, Bdl, k, g, thdt, z0, inv, inv_c, pop, pop_c;
     int Q;       // the plane basis (inspection only; kernels stop before it)
     int stage;   // leading part a kernel stages in shared memory
     int stride;
@@ -98,10 +122,12 @@ MBG_HD cvr_layout make_cvr_layout(int N)
     L.has_qm = 4;
     L.p0 = 5;
     L.nplanes = 6;
-    int o = 8;
+    int o = FDTD_END;
     L.Bd = o;
     o += L.V * L.V;
-    L.c = o;
+    L.Bdl = o;  // Bd - fl32(Bd): the FP32 kernels add it to the low word
+    o += L.V * L.V;
+    L.k = o;
     o += L.V;
     L.g = o;
     o += L.V;
@@ -143,7 +169,7 @@ MBG_HD cay_layout make_cay_layout(int N)
     L.cH = 2;
     L.gam = 3;
     L.has_qm = 4;
-    int o = 8;
+    int o = FDTD_END;
     L.kH0 = o;
     o += N * N;
     L.kMu = o;
@@ -499,6 +525,22 @@ MBG_HD void fdtd_constants(const mat_in& m, double* a, double* b, double* c)
     *c = m.dt / (MU0 * m.mu_r * m.dx);
 }
 
+// The FDTD entries of a material block (see FD_* above).
+MBG_HD void write_fdtd(const mat_in& m, double* out)
+{
+    double a, b, c;
+    fdtd_constants(m, &a, &b, &c);
+    out[FD_A] = a;
+    out[FD_B] = b;
+    out[FD_C] = c;
+    out[FD_GAMMA] = m.overlap;
+    const double bdx = b / m.dx;
+    out[FD_BDX] = bdx;
+    out[FD_BDX_LO] = bdx - (double) (float) bdx;
+    out[FD_C_LO] = c - (double) (float) c;
+    out[FD_G] = b * m.overlap;
+}
+
 // Coherence-vector constants of one material into out (cvr_layout of
 // `Nsolver` levels). Returns 0 on success, 1 when the level count does not
 // match the solver, 2 when M d_in = d_eq has no solution (the reference's
@@ -507,12 +549,7 @@ MBG_HD int cvr_precompute(const mat_in& m, int Nsolver, double* ws, double* out)
 {
     cvr_layout L = make_cvr_layout(Nsolver);
     for (int i = 0; i < L.stride; i++) out[i] = 0.0;
-    double a, b, c;
-    fdtd_constants(m, &a, &b, &c);
-    out[L.a] = a;
-    out[L.b] = b;
-    out[L.cH] = c;
-    out[L.gam] = m.overlap;
+    write_fdtd(m, out);
     const int N = Nsolver, V = L.V, KP = L.KP;
     if (m.N == 0) {
         // no quantum-mechanical description: the density stays the zero
@@ -757,50 +794,50 @@ MBG_HD int cvr_precompute(const mat_in& m, int Nsolver, double* ws, double* out)
             double s = 0.0;
             for (int k = 0; k < V; k++) s += Q[k * V + i] * H1[k * V + j];
             out[L.Bd + i * V + j] = s;
+            out[L.Bdl + i * V + j] = s - (double) (float) s;
         }
-    // c = Q^T d_in ; g = M_CP Q^T M^T v ; p0 = M_CP v^T (d_eq - M d_in)
+    // k = Q^T (A1 - I) d_in ; g = M_CP Q^T M^T v ; p0 = M_CP v^T d_eq
     for (int j = 0; j < V; j++) {
         double s = 0.0;
         for (int i = 0; i < V; i++) s += M[i * V + j] * v_dip[i];
         t1[j] = s;  // (M^T v)_j
     }
-    double p0 = 0.0;
     for (int i = 0; i < V; i++) {
-        double s = d_eq[i];
-        for (int j = 0; j < V; j++) s -= M[i * V + j] * d_in[j];
-        p0 += v_dip[i] * s;
+        double s = 0.0;
+        for (int j = 0; j < V; j++) s += F[i * V + j] * d_in[j];
+        t2[i] = s;  // F d_in
     }
+    double p0 = 0.0;
+    for (int i = 0; i < V; i++) p0 += v_dip[i] * d_eq[i];
     out[L.p0] = M_CP * p0;
     for (int k = 0; k < V; k++) {
-        double sc = 0.0, sg = 0.0;
+        double sk = 0.0, sg = 0.0;
         for (int i = 0; i < V; i++) {
-            sc += Q[i * V + k] * d_in[i];
+            sk += Q[i * V + k] * t2[i];
             sg += Q[i * V + k] * t1[i];
         }
-        out[L.c + k] = sc;
+        out[L.k + k] = sk;
         out[L.g + k] = M_CP * sg;
     }
-    // initial state z0 = Q^T (d0 + d_in)
+    // initial state u0 = Q^T d0
     initial_coherence_vector(m, d0);
     for (int k = 0; k < V; k++) {
         double s = 0.0;
-        for (int i = 0; i < V; i++) s += Q[i * V + k] * (d0[i] + d_in[i]);
+        for (int i = 0; i < V; i++) s += Q[i * V + k] * d0[i];
         out[L.z0 + k] = s;
     }
-    // observables: d = Q z - d_in
+    // observables: d = Q u
     int w0 = N * (N - 1);
     for (int k = 0; k < V; k++) out[L.inv + k] = Q[w0 * V + k];
-    out[L.inv_c] = -d_in[w0];
+    out[L.inv_c] = 0.0;
     for (int mm = 0; mm < N; mm++) {
-        double cst = population_const(N, mm);
         for (int k = 0; k < V; k++) out[L.pop + mm * V + k] = 0.0;
         for (int i = 0; i < N - 1; i++) {
             double w = 0.5 * population_weight(N, mm, i);
             for (int k = 0; k < V; k++)
                 out[L.pop + mm * V + k] += w * Q[(w0 + i) * V + k];
-            cst -= w * d_in[w0 + i];
         }
-        out[L.pop_c + mm] = cst;
+        out[L.pop_c + mm] = population_const(N, mm);
     }
     return 0;
 }
@@ -826,12 +863,7 @@ MBG_HD int cay_precompute(const mat_in& m, int Nsolver, double* ws, double* out)
 {
     cay_layout L = make_cay_layout(Nsolver);
     for (int i = 0; i < L.stride; i++) out[i] = 0.0;
-    double a, b, c;
-    fdtd_constants(m, &a, &b, &c);
-    out[L.a] = a;
-    out[L.b] = b;
-    out[L.cH] = c;
-    out[L.gam] = m.overlap;
+    write_fdtd(m, out);
     int N = Nsolver;
     if (m.N == 0) {
         out[L.has_qm] = 0.0;
@@ -873,12 +905,7 @@ MBG_HD int noop_precompute(const mat_in& m, double* out)
 {
     cvr_layout L = make_cvr_layout(0);
     for (int i = 0; i < L.stride; i++) out[i] = 0.0;
-    double a, b, c;
-    fdtd_constants(m, &a, &b, &c);
-    out[L.a] = a;
-    out[L.b] = b;
-    out[L.cH] = c;
-    out[L.gam] = m.overlap;
+    write_fdtd(m, out);
     return 0;
 }
 

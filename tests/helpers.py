@@ -65,27 +65,26 @@ def golden_cases():
     return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
 
 
-def plane_basis_step(c, L, d, d_in, e):
+def plane_basis_step(c, L, d, e):
     """One update of the engine's plane-basis form (numpy, FP64) from a
     constant block `c` with layout `L`: returns (d', P) for coherence
-    vector d, field e and the material's d_in."""
+    vector d and field e."""
     import math
     V = L["V"]
     Q = c[L["Q"]:L["Q"] + V * V].reshape(V, V)
     Bd = c[L["Bd"]:L["Bd"] + V * V].reshape(V, V)
-    cc = c[L["c"]:L["c"] + V]
+    k_ = c[L["k"]:L["k"] + V]
     g = c[L["g"]:L["g"] + V]
     th = c[L["thdt"]:L["thdt"] + V // 2]
-    z = Q.T @ (d + d_in)
-    w = z + Bd @ z - cc
+    u = Q.T @ d
+    w = u + (Bd @ u + k_)
     for k in range(V // 2):
         phi = th[k] * e
         a, b = w[2 * k], w[2 * k + 1]
         w[2 * k] = math.cos(phi) * a - math.sin(phi) * b
         w[2 * k + 1] = math.sin(phi) * a + math.cos(phi) * b
-    w = w + cc
-    z2 = w + Bd @ w
-    return Q @ z2 - d_in, c[L["p0"]] + g @ z2
+    u2 = w + (Bd @ w + k_)
+    return Q @ u2, c[L["p0"]] + g @ u2
 
 
 def tuning(C_=0, NT=0, depth=0, graph=0):

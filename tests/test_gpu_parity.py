@@ -13,8 +13,10 @@ from tests import helpers
 
 pytestmark = pytest.mark.gpu
 
-# relative L2 error per record against the reference's FP64 result
-TOL = {"fp64": 1e-9, "fp32": 2e-4}
+# relative L2 error per record against the reference's FP64 result. FP32
+# keeps E, H and the coherence vector as float pairs; the Cayley density
+# matrix is plain FP32 (renormalised trace).
+TOL = {"fp64": 1e-9, "fp32": 1e-5, "fp32-cayley": 2e-4}
 
 
 def _gpu_name(cpu_name, prec):
@@ -40,9 +42,11 @@ def test_gpu_matches_golden(native, case, prec):
     assert grid.num_timesteps == meta["num_timesteps"]
     assert sce.get_timestep_size() == meta["timestep_size"]
     errs = []
+    tol = TOL[prec + "-cayley"] if (prec == "fp32" and "cayley" in case) \
+        else TOL[prec]
     for k, (a, b) in enumerate(zip(res, recs)):
         assert a.shape == b.shape
-        errs.append(_check(a, b, TOL[prec], (case, k)))
+        errs.append(_check(a, b, tol, (case, k)))
     print(case, prec, ["%.2e" % e for e in errs])
 
 
@@ -150,13 +154,11 @@ def test_device_precompute_equals_host(native):
         L = _native.material_layout("cvr-rodr", N)
         # the plane basis is not unique (degenerate planes, null space), so
         # compare what it computes: one update from the same state
-        from oracle import oracle as O
-        d_in = O.rodr_constants(mat.qm.contents, 2e-17, 0.0)["d_in"]
         rng = np.random.default_rng(N)
         for e in (0.0, 2e8, -7e8):
             d = rng.normal(size=L["V"]) * 0.3
-            dh, ph = helpers.plane_basis_step(host, L, d, d_in, e)
-            dd, pd = helpers.plane_basis_step(devc, L, d, d_in, e)
+            dh, ph = helpers.plane_basis_step(host, L, d, e)
+            dd, pd = helpers.plane_basis_step(devc, L, d, e)
             np.testing.assert_allclose(dd, dh, rtol=0, atol=1e-12)
             # P ~ n mu omega ~ 1e10 A/m^2 for these media
             assert abs(pd - ph) <= 1e-8 * max(abs(ph), 1e10)

@@ -12,6 +12,7 @@ import scipy.linalg
 from mbsolve_gb300 import capi_types as T
 from mbsolve_gb300 import lib as mb
 from mbsolve_gb300 import setups
+from tests import helpers
 
 
 def _constants(native, algo, mat, dt):
@@ -40,11 +41,6 @@ def test_plane_basis_step_equals_dense_rodrigues(native, N, seed):
     c = _constants(native, "cvr-rodr", mat, dt)
     Q = c[L["Q"]:L["Q"] + V * V].reshape(V, V)
     np.testing.assert_allclose(Q.T @ Q, np.eye(V), atol=1e-12)
-    Bd = c[L["Bd"]:L["Bd"] + V * V].reshape(V, V)
-    cc = c[L["c"]:L["c"] + V]
-    g = c[L["g"]:L["g"] + V]
-    th = c[L["thdt"]:L["thdt"] + V // 2]
-    p0 = c[L["p0"]]
     rng = np.random.default_rng(seed)
     for e in (0.0, 3e7, -8e8):
         o = O.rodr_constants(mat.qm.contents, dt, e * dt)
@@ -54,25 +50,19 @@ def test_plane_basis_step_equals_dense_rodrigues(native, N, seed):
         d2 = o["A2"] @ d1
         dr = o["A1"] @ (d2 + o["d_in"]) - o["d_in"]
         pr = o["M_CP"] * o["v"] @ (o["M"] @ dr + o["d_eq"])
-        # plane-basis update
-        z = Q.T @ (d + o["d_in"])
-        w = z + Bd @ z - cc
-        for k in range(V // 2):
-            phi = th[k] * e
-            a, bb = w[2 * k], w[2 * k + 1]
-            w[2 * k] = math.cos(phi) * a - math.sin(phi) * bb
-            w[2 * k + 1] = math.sin(phi) * a + math.cos(phi) * bb
-        w = w + cc
-        z2 = w + Bd @ w
-        dg = Q @ z2 - o["d_in"]
-        pg = p0 + g @ z2
+        # plane-basis update of the engine
+        dg, pg = helpers.plane_basis_step(c, L, d, e)
         np.testing.assert_allclose(dg, dr, rtol=0, atol=1e-12)
         assert abs(pg - pr) <= 1e-10 * max(1.0, abs(pr)) + 1e-6 * abs(
             o["M_CP"] * o["v"] @ (np.abs(o["M"]) @ np.abs(dr)))
+    # the low words are the FP32 rounding errors of Bd
+    Bd = c[L["Bd"]:L["Bd"] + V * V]
+    Bdl = c[L["Bdl"]:L["Bdl"] + V * V]
+    np.testing.assert_array_equal(Bd - Bd.astype(np.float32).astype(np.float64), Bdl)
     # observables: inversion is d[N(N-1)]
     d = rng.normal(size=V)
-    z = Q.T @ (d + o["d_in"])
-    inv = c[L["inv"]:L["inv"] + V] @ z + c[L["inv_c"]]
+    u = Q.T @ d
+    inv = c[L["inv"]:L["inv"] + V] @ u + c[L["inv_c"]]
     assert abs(inv - d[N * (N - 1)]) < 1e-12
 
 
