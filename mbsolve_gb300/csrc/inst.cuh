@@ -3,6 +3,7 @@
 #pragma once
 
 #include "engine.hpp"
+#include "tile_kernel.cuh"
 
 namespace mbg {
 

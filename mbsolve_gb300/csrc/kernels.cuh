@@ -228,20 +228,58 @@ __device__ __forceinline__ void cvr_update(T (&u)[V], T e, T& pout, const CF& cf
     pout = pp;
 }
 
-// hi + lo <- hi + lo + d (TwoSum, then renormalised)
+// hi + lo <- hi + lo + d, TwoSum without renormalising: lo collects the
+// exact rounding error of the high word (and extra_lo)
 __device__ __forceinline__ void df_acc(float& h, float& l, float d, float extra_lo)
 {
     const float s = h + d;
     const float bv = s - h;
     const float err = (h - (s - bv)) + (d - bv);
-    const float e2 = l + err + extra_lo;
-    h = s + e2;
-    l = e2 - (h - s);
+    h = s;
+    l = l + (err + extra_lo);
 }
+
+// renormalise a pair so that |lo| <= ulp(hi)/2 (Fast2Sum)
+__device__ __forceinline__ void df_renorm(float& h, float& l)
+{
+    const float s = h + l;
+    l = l - (s - h);
+    h = s;
+}
+
+// Coefficients of the 2-level update held in registers (uniform tiles).
+template<typename T, int V>
+struct cvr_coef_reg {
+    T bd[V * V], bdl[V * V], kk[V], gg[V], thv[V / 2 > 0 ? V / 2 : 1], pz;
+    __device__ __forceinline__ explicit cvr_coef_reg(const T* base)
+    {
+        cvr_coef<T, V> c{ base };
+#pragma unroll
+        for (int i = 0; i < V; i++) {
+#pragma unroll
+            for (int j = 0; j < V; j++) {
+                bd[i * V + j] = c.Bd(i, j);
+                bdl[i * V + j] = c.Bdl(i, j);
+            }
+            kk[i] = c.k(i);
+            gg[i] = c.g(i);
+        }
+#pragma unroll
+        for (int q = 0; q < V / 2; q++) thv[q] = c.th(q);
+        pz = c.p0();
+    }
+    __device__ __forceinline__ T Bd(int i, int j) const { return bd[i * V + j]; }
+    __device__ __forceinline__ T Bdl(int i, int j) const { return bdl[i * V + j]; }
+    __device__ __forceinline__ T k(int i) const { return kk[i]; }
+    __device__ __forceinline__ T g(int i) const { return gg[i]; }
+    __device__ __forceinline__ T th(int q) const { return thv[q]; }
+    __device__ __forceinline__ T p0() const { return pz; }
+};
 
 // The same update in FP32 with u = uh + ul: the corrections are computed in
 // FP32 from the high words and accumulated error-free; the low words take
-// the rounding errors and the Bdl contribution.
+// the rounding errors and the Bdl contribution; one renormalisation per
+// step.
 template<int V, class CF>
 __device__ __forceinline__ void cvr_update_df(float (&uh)[V], float (&ul)[V], float e, float& pout, const CF& cf)
 {
@@ -280,6 +318,7 @@ __device__ __forceinline__ void cvr_update_df(float (&uh)[V], float (&ul)[V], fl
         uh[i] = wh[i];
         ul[i] = wl[i];
         df_acc(uh[i], ul[i], c, cl);
+        df_renorm(uh[i], ul[i]);
         pp = fmaf(cf.g(i), uh[i], fmaf(cf.g(i), ul[i], pp));
     }
     pout = pp;
@@ -663,313 +702,6 @@ __device__ __forceinline__ void cayley_update(T (&rho)[N * N], T e, T& pout, con
             acc += r.re * Mn[k][j].re - r.im * Mn[k][j].im;
         }
     pout = acc;
-}
-
-// ------------------------------------------------------- the tile kernel
-//
-// ALGO 0: Maxwell only (algo_lindblad_noop.hpp), 1: coherence vector /
-// Rodrigues, 2: Cayley. D density reals per point: 0, N^2 - 1, N^2.
-
-template<int ALGO, int LEV>
-struct density_len {
-    static constexpr int value = ALGO == 1 ? LEV * LEV - 1 : ALGO == 2 ? LEV * LEV : 0;
-};
-
-template<typename T, int ALGO, int LEV, int C, int NT, bool UNIFORM>
-__device__ __forceinline__ void tile_steps(
-    const kparams<T>& p,
-    const tile_desc& td,
-    const run_desc& rd,
-    int64_t l0,
-    int nsteps,
-    uint64_t step0,
-    T (&E)[C],
-    T (&El)[C],
-    T (&H)[C],
-    T (&Hl)[C],
-    T (&P)[C],
-    T (&R)[C][density_len<ALGO, LEV>::value > 0 ? density_len<ALGO, LEV>::value : 1],
-    T (&Rl)[C][density_len<ALGO, LEV>::value > 0 ? density_len<ALGO, LEV>::value : 1],
-    const int32_t (&M)[C],
-    const T* sh_coef,
-    T* sh_a,
-    T* sh_al,
-    T* sh_b,
-    T* sh_bl)
-{
-    constexpr bool DF = sizeof(T) == 4;
-    constexpr int D = density_len<ALGO, LEV>::value;
-    constexpr int NW = NT / 32;
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int64_t nx = rd.n_x;
-    const T dxi = (T) rd.dx_inv;
-    // coefficient block of point j
-    auto block = [&](int j) -> const T* {
-        return UNIFORM ? sh_coef : p.mc + (uint64_t) (M[j] >= 0 ? M[j] : 0) * p.mstride;
-    };
-    fcoef fu;
-    if constexpr (DF && UNIFORM) fu = load_fcoef(sh_coef);
-
-    for (int m = 0; m < nsteps; m++) {
-        const uint64_t n = step0 + (uint64_t) m;
-        // ---- E: needs H (hi, lo) of the right neighbour
-        if (lane == 0) {
-            sh_a[warp] = H[0];
-            if constexpr (DF) sh_al[warp] = Hl[0];
-        }
-        __syncthreads();
-        T hr = __shfl_down_sync(0xffffffffu, H[0], 1);
-        T hrl = DF ? __shfl_down_sync(0xffffffffu, Hl[0], 1) : T(0);
-        if (lane == 31) {
-            hr = (warp + 1 < NW) ? sh_a[warp + 1] : T(0);
-            if constexpr (DF) hrl = (warp + 1 < NW) ? sh_al[warp + 1] : T(0);
-        }
-#pragma unroll
-        for (int j = 0; j < C; j++) {
-            if (M[j] < 0) continue;
-            const T hn = (j + 1 < C) ? H[j + 1] : hr;
-            if constexpr (DF) {
-                const T hnl = (j + 1 < C) ? Hl[j + 1] : hrl;
-                const fcoef f = UNIFORM ? fu : load_fcoef(block(j));
-                df_e_update(E[j], El[j], hn - H[j], hnl - Hl[j], P[j], f);
-            } else {
-                const T* cb = block(j);
-                E[j] = cb[pre::FD_A] * E[j] +
-                    cb[pre::FD_B] * (-cb[pre::FD_GAMMA] * P[j] + (hn - H[j]) * dxi);
-            }
-        }
-        // ---- sources, after E and before H (solver_cpu_fdtd.tpp:245-255)
-        for (uint32_t s = rd.src_begin; s < rd.src_end; s++) {
-            const src_desc sd = p.srcs[s];
-            const int64_t jj = (int64_t) sd.x_idx - l0;
-            if (jj >= 0 && jj < C) {
-                const double v = p.stab[sd.table_offset + n];
-#pragma unroll
-                for (int j = 0; j < C; j++) {
-                    if (j != jj || M[j] < 0) continue;
-                    if (sd.type == 0) {
-                        E[j] = (T) v;
-                        if constexpr (DF) El[j] = (T) (v - (double) E[j]);
-                    } else {
-                        if constexpr (DF)
-                            df_add(E[j], El[j], v);
-                        else
-                            E[j] += (T) v;
-                    }
-                }
-            }
-        }
-        // ---- H: needs E (hi, lo) of the left neighbour
-        if (lane == 31) {
-            sh_b[warp] = E[C - 1];
-            if constexpr (DF) sh_bl[warp] = El[C - 1];
-        }
-        __syncthreads();
-        T el = __shfl_up_sync(0xffffffffu, E[C - 1], 1);
-        T ell = DF ? __shfl_up_sync(0xffffffffu, El[C - 1], 1) : T(0);
-        if (lane == 0) {
-            el = (warp > 0) ? sh_b[warp - 1] : T(0);
-            if constexpr (DF) ell = (warp > 0) ? sh_bl[warp - 1] : T(0);
-        }
-#pragma unroll
-        for (int j = 0; j < C; j++) {
-            const int64_t l = l0 + j;
-            if (l >= 1 && l < nx) {
-                const T ep = (j > 0) ? E[j - 1] : el;
-                if constexpr (DF) {
-                    const T epl = (j > 0) ? El[j - 1] : ell;
-                    const fcoef f = UNIFORM ? fu : load_fcoef(block(j));
-                    df_h_update(H[j], Hl[j], E[j] - ep, El[j] - epl, f);
-                } else {
-                    H[j] += block(j)[pre::FD_C] * (E[j] - ep);
-                }
-            } else if (l == 0) {
-                H[j] = T(0);
-                if constexpr (DF) Hl[j] = T(0);
-            }
-        }
-        // ---- density matrix and polarisation current at every point
-        if constexpr (D > 0) {
-#pragma unroll
-            for (int j = 0; j < C; j++) {
-                if (M[j] < 0) continue;
-                const T* cb = block(j);
-                if (cb[pre::FD_HAS_QM] == T(0)) continue;
-                const T e = DF ? E[j] + El[j] : E[j];
-                if constexpr (ALGO == 1) {
-                    cvr_coef<T, D> cf{ cb };
-                    if constexpr (DF)
-                        cvr_update_df<D>(R[j], Rl[j], e, P[j], cf);
-                    else
-                        cvr_update<T, D>(R[j], e, P[j], cf);
-                } else {
-                    cayley_update<T, LEV>(R[j], e, P[j], cb);
-                }
-            }
-        }
-        // ---- recording (solver_cpu_fdtd.tpp:288-325)
-        if (p.record) {
-            for (uint32_t r = rd.rec_begin; r < rd.rec_end; r++) {
-                const rec_desc rc = p.recs[r];
-                if (!hasto_record(rc.ratio, n)) continue;
-                const int64_t lo = max((int64_t) rc.pos, (int64_t) td.out_start);
-                const int64_t hi = min((int64_t) rc.pos + rc.cols, (int64_t) td.out_start + td.out_len);
-                if (l0 + C <= lo || l0 >= hi) continue;
-#pragma unroll
-                for (int j = 0; j < C; j++) {
-                    const int64_t l = l0 + j;
-                    if (l < lo || l >= hi) continue;
-                    const T ev = DF ? E[j] + El[j] : E[j];
-                    const T hv = DF ? H[j] + Hl[j] : H[j];
-                    T v = T(0);
-                    if constexpr (ALGO == 2) {
-                        switch (rc.type) {
-                        case 0: v = ev; break;
-                        case 1: v = P[j]; break;
-                        case 2: v = hv; break;
-                        case 4: v = R[j][1] - R[j][0]; break;
-                        case 3:
-                            if (rc.row_idx == rc.col_idx && rc.row_idx < (uint32_t) LEV) v = R[j][rc.row_idx];
-                            break;
-                        }
-                    } else {
-                        constexpr int DDv = D > 0 ? D : 1;
-                        T u[DDv];
-#pragma unroll
-                        for (int q = 0; q < DDv; q++) u[q] = DF ? R[j][q] + Rl[j][q] : R[j][q];
-                        v = cvr_record_value<T, D>(rc, ev, hv, P[j], u, block(j), LEV);
-                    }
-                    store_record<T>(p, rc, n, l, v);
-                }
-            }
-        }
-    }
-}
-
-template<typename T, int ALGO, int LEV, int C, int NT>
-__global__ void __launch_bounds__(NT) step_kernel(const kparams<T> p)
-{
-    constexpr bool DF = sizeof(T) == 4;
-    constexpr int D = density_len<ALGO, LEV>::value;
-    constexpr int DD = D > 0 ? D : 1;
-    constexpr int NW = NT / 32;
-    __shared__ T sh_a[NW], sh_al[NW], sh_b[NW], sh_bl[NW];
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sh_coef = reinterpret_cast<T*>(smem_raw);
-
-    const tile_desc td = p.tiles[blockIdx.x];
-    const run_desc rd = p.runs[td.run];
-    const int64_t l0 = (int64_t) td.out_start - (int64_t) p.halo + (int64_t) threadIdx.x * C;
-    const int64_t g0 = (int64_t) rd.offset + l0;
-    const int64_t nx = rd.n_x;
-    const uint64_t step0 = *p.step_base + (uint64_t) p.launch_idx * p.depth;
-    int nsteps = 0;
-    if (step0 < rd.n_t) nsteps = (int) min((uint64_t) p.nsub, (uint64_t) rd.n_t - step0);
-
-    T E[C], El[C], H[C], Hl[C], P[C];
-    T R[C][DD];
-    T Rl[C][DD];  // FP32 coherence vector: low words
-    constexpr bool DFD = DF && ALGO == 1;
-    int32_t M[C];
-    load_cells<T, C>(E, p.Ein, g0);
-    load_cells<T, C>(H, p.Hin, g0);
-    load_cells<T, C>(P, p.Pin, g0);
-    if constexpr (DF) {
-        load_cells<T, C>(El, p.Elin, g0);
-        load_cells<T, C>(Hl, p.Hlin, g0);
-    }
-    if constexpr (D > 0) {
-#pragma unroll
-        for (int v = 0; v < D; v++) {
-            T tmp[C];
-            load_cells<T, C>(tmp, p.Din + (uint64_t) v * p.plane, g0);
-#pragma unroll
-            for (int j = 0; j < C; j++) R[j][v] = tmp[j];
-            if constexpr (DFD) {
-                load_cells<T, C>(tmp, p.Din + (uint64_t) (D + v) * p.plane, g0);
-#pragma unroll
-                for (int j = 0; j < C; j++) Rl[j][v] = tmp[j];
-            }
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < C; j++) {
-        if constexpr (!DFD)
-#pragma unroll
-            for (int v = 0; v < DD; v++) Rl[j][v] = T(0);
-        const int64_t l = l0 + j;
-        const bool valid = (l >= 0) && (l < nx);
-        M[j] = valid ? __ldg(p.mat + g0 + j) : -1;
-        if (!valid) {
-            E[j] = H[j] = P[j] = T(0);
-            El[j] = Hl[j] = T(0);
-#pragma unroll
-            for (int v = 0; v < DD; v++) R[j][v] = Rl[j][v] = T(0);
-        }
-        if constexpr (!DF) El[j] = Hl[j] = T(0);
-    }
-    const bool uniform = td.uniform_mat >= 0;
-    if (uniform) {
-        const T* src = p.mc + (uint64_t) td.uniform_mat * p.mstride;
-        for (int i = threadIdx.x; i < (int) p.mstage; i += NT) sh_coef[i] = src[i];
-    }
-    __syncthreads();
-
-    if (uniform)
-        tile_steps<T, ALGO, LEV, C, NT, true>(p, td, rd, l0, nsteps, step0, E, El, H, Hl, P, R, Rl, M,
-                                              sh_coef, sh_a, sh_al, sh_b, sh_bl);
-    else
-        tile_steps<T, ALGO, LEV, C, NT, false>(p, td, rd, l0, nsteps, step0, E, El, H, Hl, P, R, Rl, M,
-                                               sh_coef, sh_a, sh_al, sh_b, sh_bl);
-
-    // Cayley, FP32: renormalise the trace to that of the initial density
-    // matrix, in FP64, once per launch (the exact propagators preserve it:
-    // the scattering matrix has zero column sums and U2 is unitary; this
-    // removes FP32 round-off drift)
-    if constexpr (ALGO == 2 && DF) {
-        const pre::cay_layout L = pre::make_cay_layout(LEV);
-#pragma unroll
-        for (int j = 0; j < C; j++) {
-            if (M[j] < 0 || nsteps == 0) continue;
-            const T* cb = uniform ? sh_coef : p.mc + (uint64_t) M[j] * p.mstride;
-            if (cb[pre::FD_HAS_QM] == T(0)) continue;
-            double tr = 0.0, target = 0.0;
-#pragma unroll
-            for (int i = 0; i < LEV; i++) {
-                tr += (double) R[j][i];
-                target += (double) cb[L.rho0 + i];
-            }
-            if (tr != 0.0 && fabs(tr / target - 1.0) < 1e-3) {
-                const float s = (float) (target / tr);
-#pragma unroll
-                for (int v = 0; v < DD; v++) R[j][v] *= s;
-            }
-        }
-    }
-
-    const int64_t lo = td.out_start, hi = (int64_t) td.out_start + td.out_len;
-    store_cells<T, C>(E, p.Eout, g0, l0, lo, hi);
-    store_cells<T, C>(H, p.Hout, g0, l0, lo, hi);
-    store_cells<T, C>(P, p.Pout, g0, l0, lo, hi);
-    if constexpr (DF) {
-        store_cells<T, C>(El, p.Elout, g0, l0, lo, hi);
-        store_cells<T, C>(Hl, p.Hlout, g0, l0, lo, hi);
-    }
-    if constexpr (D > 0) {
-#pragma unroll
-        for (int v = 0; v < D; v++) {
-            T tmp[C];
-#pragma unroll
-            for (int j = 0; j < C; j++) tmp[j] = R[j][v];
-            store_cells<T, C>(tmp, p.Dout + (uint64_t) v * p.plane, g0, l0, lo, hi);
-            if constexpr (DFD) {
-#pragma unroll
-                for (int j = 0; j < C; j++) tmp[j] = Rl[j][v];
-                store_cells<T, C>(tmp, p.Dout + (uint64_t) (D + v) * p.plane, g0, l0, lo, hi);
-            }
-        }
-    }
 }
 
 }  // namespace mbg

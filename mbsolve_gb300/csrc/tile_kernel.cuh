@@ -1,0 +1,380 @@
+// The tile kernel: one launch advances every tile of every run by up to
+// `nsub` time steps (see kernels.cuh for the scheme and the per-point
+// updates).
+//
+// ALGO 0: Maxwell only (algo_lindblad_noop.hpp), 1: coherence vector /
+// Rodrigues, 2: Cayley. D density reals per point: 0, N^2 - 1, N^2.
+#pragma once
+
+#include <type_traits>
+
+#include "kernels.cuh"
+
+namespace mbg {
+
+template<int ALGO, int LEV>
+struct density_len {
+    static constexpr int value = ALGO == 1 ? LEV * LEV - 1 : ALGO == 2 ? LEV * LEV : 0;
+};
+
+// sources and records that touch one tile, gathered once per launch
+constexpr int TILE_MAX_SRC = 8;
+constexpr int TILE_MAX_REC = 8;
+
+struct no_coef {
+    __device__ __forceinline__ explicit no_coef(const void*) {}
+};
+
+struct tile_lists {
+    int nsrc, nrec, overflow;
+    src_desc src[TILE_MAX_SRC];
+    rec_desc rec[TILE_MAX_REC];
+};
+
+template<typename T, int ALGO, int LEV, int C, int NT, bool UNIFORM>
+__device__ __forceinline__ void tile_steps(
+    const kparams<T>& p,
+    const tile_desc& td,
+    const run_desc& rd,
+    int64_t l0,
+    int nsteps,
+    uint64_t step0,
+    T (&E)[C],
+    T (&El)[C],
+    T (&H)[C],
+    T (&Hl)[C],
+    T (&P)[C],
+    T (&R)[C][density_len<ALGO, LEV>::value > 0 ? density_len<ALGO, LEV>::value : 1],
+    T (&Rl)[C][density_len<ALGO, LEV>::value > 0 ? density_len<ALGO, LEV>::value : 1],
+    const int32_t (&M)[C],
+    const T* sh_coef,
+    const tile_lists& tl,
+    T* sh_a,
+    T* sh_al,
+    T* sh_b,
+    T* sh_bl)
+{
+    constexpr bool DF = sizeof(T) == 4;
+    constexpr int D = density_len<ALGO, LEV>::value;
+    constexpr int NW = NT / 32;
+    // 2-level coefficients live in registers on uniform tiles
+    constexpr bool REGCOEF = UNIFORM && ALGO == 1 && D == 3;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int64_t nx = rd.n_x;
+    const T dxi = (T) rd.dx_inv;
+    auto block = [&](int j) -> const T* {
+        return UNIFORM ? sh_coef : p.mc + (uint64_t) (M[j] >= 0 ? M[j] : 0) * p.mstride;
+    };
+    fcoef fu;
+    if constexpr (DF && UNIFORM) fu = load_fcoef(sh_coef);
+    const bool qm_uniform = UNIFORM && sh_coef[pre::FD_HAS_QM] != T(0);
+    using creg_t = typename std::conditional<REGCOEF, cvr_coef_reg<T, 3>, no_coef>::type;
+    const creg_t creg(sh_coef);
+    const int nsrc = tl.overflow ? (int) (rd.src_end - rd.src_begin) : tl.nsrc;
+    const int nrec = tl.overflow ? (int) (rd.rec_end - rd.rec_begin) : tl.nrec;
+
+    for (int m = 0; m < nsteps; m++) {
+        const uint64_t n = step0 + (uint64_t) m;
+        // ---- E: needs H (hi, lo) of the right neighbour
+        if (lane == 0) {
+            sh_a[warp] = H[0];
+            if constexpr (DF) sh_al[warp] = Hl[0];
+        }
+        __syncthreads();
+        T hr = __shfl_down_sync(0xffffffffu, H[0], 1);
+        T hrl = DF ? __shfl_down_sync(0xffffffffu, Hl[0], 1) : T(0);
+        if (lane == 31) {
+            hr = (warp + 1 < NW) ? sh_a[warp + 1] : T(0);
+            if constexpr (DF) hrl = (warp + 1 < NW) ? sh_al[warp + 1] : T(0);
+        }
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            if (M[j] < 0) continue;
+            const T hn = (j + 1 < C) ? H[j + 1] : hr;
+            if constexpr (DF) {
+                const T hnl = (j + 1 < C) ? Hl[j + 1] : hrl;
+                const fcoef f = UNIFORM ? fu : load_fcoef(block(j));
+                df_e_update(E[j], El[j], hn - H[j], hnl - Hl[j], P[j], f);
+            } else {
+                const T* cb = block(j);
+                E[j] = cb[pre::FD_A] * E[j] +
+                    cb[pre::FD_B] * (-cb[pre::FD_GAMMA] * P[j] + (hn - H[j]) * dxi);
+            }
+        }
+        // ---- sources, after E and before H (solver_cpu_fdtd.tpp:245-255)
+        for (int s = 0; s < nsrc; s++) {
+            const src_desc sd = tl.overflow ? p.srcs[rd.src_begin + s] : tl.src[s];
+            const int64_t jj = (int64_t) sd.x_idx - l0;
+            if (jj >= 0 && jj < C) {
+                const double v = p.stab[sd.table_offset + n];
+#pragma unroll
+                for (int j = 0; j < C; j++) {
+                    if (j != jj || M[j] < 0) continue;
+                    if (sd.type == 0) {
+                        E[j] = (T) v;
+                        if constexpr (DF) El[j] = (T) (v - (double) E[j]);
+                    } else {
+                        if constexpr (DF)
+                            df_add(E[j], El[j], v);
+                        else
+                            E[j] += (T) v;
+                    }
+                }
+            }
+        }
+        // ---- H: needs E (hi, lo) of the left neighbour
+        if (lane == 31) {
+            sh_b[warp] = E[C - 1];
+            if constexpr (DF) sh_bl[warp] = El[C - 1];
+        }
+        __syncthreads();
+        T el = __shfl_up_sync(0xffffffffu, E[C - 1], 1);
+        T ell = DF ? __shfl_up_sync(0xffffffffu, El[C - 1], 1) : T(0);
+        if (lane == 0) {
+            el = (warp > 0) ? sh_b[warp - 1] : T(0);
+            if constexpr (DF) ell = (warp > 0) ? sh_bl[warp - 1] : T(0);
+        }
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            const int64_t l = l0 + j;
+            if (l >= 1 && l < nx) {
+                const T ep = (j > 0) ? E[j - 1] : el;
+                if constexpr (DF) {
+                    const T epl = (j > 0) ? El[j - 1] : ell;
+                    const fcoef f = UNIFORM ? fu : load_fcoef(block(j));
+                    df_h_update(H[j], Hl[j], E[j] - ep, El[j] - epl, f);
+                } else {
+                    H[j] += block(j)[pre::FD_C] * (E[j] - ep);
+                }
+            } else if (l == 0) {
+                H[j] = T(0);
+                if constexpr (DF) Hl[j] = T(0);
+            }
+        }
+        // ---- density matrix and polarisation current at every point
+        if constexpr (D > 0) {
+#pragma unroll
+            for (int j = 0; j < C; j++) {
+                if (M[j] < 0) continue;
+                const T* cb = block(j);
+                if (UNIFORM ? !qm_uniform : cb[pre::FD_HAS_QM] == T(0)) continue;
+                const T e = DF ? E[j] + El[j] : E[j];
+                if constexpr (ALGO == 1) {
+                    if constexpr (REGCOEF) {
+                        if constexpr (DF)
+                            cvr_update_df<D>(R[j], Rl[j], e, P[j], creg);
+                        else
+                            cvr_update<T, D>(R[j], e, P[j], creg);
+                    } else {
+                        cvr_coef<T, D> cf{ cb };
+                        if constexpr (DF)
+                            cvr_update_df<D>(R[j], Rl[j], e, P[j], cf);
+                        else
+                            cvr_update<T, D>(R[j], e, P[j], cf);
+                    }
+                } else {
+                    cayley_update<T, LEV>(R[j], e, P[j], cb);
+                }
+            }
+        }
+        // ---- recording (solver_cpu_fdtd.tpp:288-325)
+        if (p.record) {
+            for (int r = 0; r < nrec; r++) {
+                const rec_desc rc = tl.overflow ? p.recs[rd.rec_begin + r] : tl.rec[r];
+                // every-step records (ratio 1) need no FP64 arithmetic
+                if (rc.ratio != 1.0 && !hasto_record(rc.ratio, n)) continue;
+                const int64_t lo = max((int64_t) rc.pos, (int64_t) td.out_start);
+                const int64_t hi = min((int64_t) rc.pos + rc.cols, (int64_t) td.out_start + td.out_len);
+                if (l0 + C <= lo || l0 >= hi) continue;
+#pragma unroll
+                for (int j = 0; j < C; j++) {
+                    const int64_t l = l0 + j;
+                    if (l < lo || l >= hi) continue;
+                    const T ev = DF ? E[j] + El[j] : E[j];
+                    const T hv = DF ? H[j] + Hl[j] : H[j];
+                    T v = T(0);
+                    if constexpr (ALGO == 2) {
+                        switch (rc.type) {
+                        case 0: v = ev; break;
+                        case 1: v = P[j]; break;
+                        case 2: v = hv; break;
+                        case 4: v = R[j][1] - R[j][0]; break;
+                        case 3:
+                            if (rc.row_idx == rc.col_idx && rc.row_idx < (uint32_t) LEV) v = R[j][rc.row_idx];
+                            break;
+                        }
+                    } else {
+                        constexpr int DDv = D > 0 ? D : 1;
+                        T u[DDv];
+#pragma unroll
+                        for (int q = 0; q < DDv; q++) u[q] = DF ? R[j][q] + Rl[j][q] : R[j][q];
+                        v = cvr_record_value<T, D>(rc, ev, hv, P[j], u, block(j), LEV);
+                    }
+                    const uint64_t row = rc.ratio == 1.0 ? n : (uint64_t) floor(rc.ratio * (double) n);
+                    if (row < rc.rows) {
+                        p.scratch[rc.offset + row * rc.cols + (uint64_t) (l - rc.pos)] = v;
+                        if (!isfinite(v)) atomicOr(p.status, STATUS_NONFINITE);
+                    }
+                }
+            }
+        }
+    }
+}
+
+template<typename T, int ALGO, int LEV, int C, int NT>
+__global__ void __launch_bounds__(NT) step_kernel(const kparams<T> p)
+{
+    constexpr bool DF = sizeof(T) == 4;
+    constexpr int D = density_len<ALGO, LEV>::value;
+    constexpr int DD = D > 0 ? D : 1;
+    constexpr int NW = NT / 32;
+    constexpr bool DFD = DF && ALGO == 1;
+    __shared__ T sh_a[NW], sh_al[NW], sh_b[NW], sh_bl[NW];
+    __shared__ tile_lists tl;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sh_coef = reinterpret_cast<T*>(smem_raw);
+
+    const tile_desc td = p.tiles[blockIdx.x];
+    const run_desc rd = p.runs[td.run];
+    const int64_t l0 = (int64_t) td.out_start - (int64_t) p.halo + (int64_t) threadIdx.x * C;
+    const int64_t g0 = (int64_t) rd.offset + l0;
+    const int64_t nx = rd.n_x;
+    const uint64_t step0 = *p.step_base + (uint64_t) p.launch_idx * p.depth;
+    int nsteps = 0;
+    if (step0 < rd.n_t) nsteps = (int) min((uint64_t) p.nsub, (uint64_t) rd.n_t - step0);
+
+    // sources inside the tile's window (halo included: the halo points
+    // must see them too) and records inside its output range
+    if (threadIdx.x == 0) {
+        const int64_t w0 = (int64_t) td.out_start - (int64_t) p.halo;
+        const int64_t w1 = w0 + (int64_t) NT * C;
+        int ns = 0, nr = 0, of = 0;
+        for (uint32_t s = rd.src_begin; s < rd.src_end; s++) {
+            const src_desc sd = p.srcs[s];
+            if ((int64_t) sd.x_idx < w0 || (int64_t) sd.x_idx >= w1) continue;
+            if (ns < TILE_MAX_SRC)
+                tl.src[ns++] = sd;
+            else
+                of = 1;
+        }
+        for (uint32_t r = rd.rec_begin; r < rd.rec_end; r++) {
+            const rec_desc rc = p.recs[r];
+            const int64_t lo = max((int64_t) rc.pos, (int64_t) td.out_start);
+            const int64_t hi = min((int64_t) rc.pos + rc.cols, (int64_t) td.out_start + td.out_len);
+            if (lo >= hi) continue;
+            if (nr < TILE_MAX_REC)
+                tl.rec[nr++] = rc;
+            else
+                of = 1;
+        }
+        tl.nsrc = ns;
+        tl.nrec = nr;
+        tl.overflow = of;
+    }
+
+    T E[C], El[C], H[C], Hl[C], P[C];
+    T R[C][DD];
+    T Rl[C][DD];  // FP32 coherence vector: low words
+    int32_t M[C];
+    load_cells<T, C>(E, p.Ein, g0);
+    load_cells<T, C>(H, p.Hin, g0);
+    load_cells<T, C>(P, p.Pin, g0);
+    if constexpr (DF) {
+        load_cells<T, C>(El, p.Elin, g0);
+        load_cells<T, C>(Hl, p.Hlin, g0);
+    }
+    if constexpr (D > 0) {
+#pragma unroll
+        for (int v = 0; v < D; v++) {
+            T tmp[C];
+            load_cells<T, C>(tmp, p.Din + (uint64_t) v * p.plane, g0);
+#pragma unroll
+            for (int j = 0; j < C; j++) R[j][v] = tmp[j];
+            if constexpr (DFD) {
+                load_cells<T, C>(tmp, p.Din + (uint64_t) (D + v) * p.plane, g0);
+#pragma unroll
+                for (int j = 0; j < C; j++) Rl[j][v] = tmp[j];
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < C; j++) {
+        if constexpr (!DFD)
+#pragma unroll
+            for (int v = 0; v < DD; v++) Rl[j][v] = T(0);
+        const int64_t l = l0 + j;
+        const bool valid = (l >= 0) && (l < nx);
+        M[j] = valid ? __ldg(p.mat + g0 + j) : -1;
+        if (!valid) {
+            E[j] = H[j] = P[j] = T(0);
+            El[j] = Hl[j] = T(0);
+#pragma unroll
+            for (int v = 0; v < DD; v++) R[j][v] = Rl[j][v] = T(0);
+        }
+        if constexpr (!DF) El[j] = Hl[j] = T(0);
+    }
+    const bool uniform = td.uniform_mat >= 0;
+    if (uniform) {
+        const T* src = p.mc + (uint64_t) td.uniform_mat * p.mstride;
+        for (int i = threadIdx.x; i < (int) p.mstage; i += NT) sh_coef[i] = src[i];
+    }
+    __syncthreads();
+
+    if (uniform)
+        tile_steps<T, ALGO, LEV, C, NT, true>(p, td, rd, l0, nsteps, step0, E, El, H, Hl, P, R, Rl, M,
+                                              sh_coef, tl, sh_a, sh_al, sh_b, sh_bl);
+    else
+        tile_steps<T, ALGO, LEV, C, NT, false>(p, td, rd, l0, nsteps, step0, E, El, H, Hl, P, R, Rl, M,
+                                               sh_coef, tl, sh_a, sh_al, sh_b, sh_bl);
+
+    // Cayley, FP32: renormalise the trace to that of the initial density
+    // matrix, in FP64, once per launch (the exact propagators preserve it:
+    // the scattering matrix has zero column sums and U2 is unitary; this
+    // removes FP32 round-off drift)
+    if constexpr (ALGO == 2 && DF) {
+        const pre::cay_layout L = pre::make_cay_layout(LEV);
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            if (M[j] < 0 || nsteps == 0) continue;
+            const T* cb = uniform ? sh_coef : p.mc + (uint64_t) M[j] * p.mstride;
+            if (cb[pre::FD_HAS_QM] == T(0)) continue;
+            double tr = 0.0, target = 0.0;
+#pragma unroll
+            for (int i = 0; i < LEV; i++) {
+                tr += (double) R[j][i];
+                target += (double) cb[L.rho0 + i];
+            }
+            if (tr != 0.0 && fabs(tr / target - 1.0) < 1e-3) {
+                const float s = (float) (target / tr);
+#pragma unroll
+                for (int v = 0; v < DD; v++) R[j][v] *= s;
+            }
+        }
+    }
+
+    const int64_t lo = td.out_start, hi = (int64_t) td.out_start + td.out_len;
+    store_cells<T, C>(E, p.Eout, g0, l0, lo, hi);
+    store_cells<T, C>(H, p.Hout, g0, l0, lo, hi);
+    store_cells<T, C>(P, p.Pout, g0, l0, lo, hi);
+    if constexpr (DF) {
+        store_cells<T, C>(El, p.Elout, g0, l0, lo, hi);
+        store_cells<T, C>(Hl, p.Hlout, g0, l0, lo, hi);
+    }
+    if constexpr (D > 0) {
+#pragma unroll
+        for (int v = 0; v < D; v++) {
+            T tmp[C];
+#pragma unroll
+            for (int j = 0; j < C; j++) tmp[j] = R[j][v];
+            store_cells<T, C>(tmp, p.Dout + (uint64_t) v * p.plane, g0, l0, lo, hi);
+            if constexpr (DFD) {
+#pragma unroll
+                for (int j = 0; j < C; j++) tmp[j] = Rl[j][v];
+                store_cells<T, C>(tmp, p.Dout + (uint64_t) (D + v) * p.plane, g0, l0, lo, hi);
+            }
+        }
+    }
+}
+
+}  // namespace mbg
