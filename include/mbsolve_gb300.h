@@ -336,6 +336,28 @@ int mbg_material_constants(
     size_t cap,
     size_t* len);
 
+/* Allocation-free variant of mbg_material_constants (no counterpart in the
+ * reference). For callers that cannot call cudaMalloc: their device memory
+ * belongs to another allocator (a framework's pool, or memory reserved up
+ * front), or the path cannot take the device-wide synchronisation that
+ * cudaMalloc/cudaFree imply. The constant block is computed on the current
+ * device into `out_device`, a device buffer of `cap` doubles the caller
+ * owns, on `stream` (NULL: the legacy default stream); the call returns
+ * when it is done. The FP64 workspace is a fixed array of about 160 KB in
+ * this library's device memory (enough for 6 levels); larger workspaces
+ * are refused with MBG_ERR_INVALID_ARGUMENT. The first call on a device
+ * looks up the array's device address; make that call before any stream
+ * capture. Every call uses the same array: calls that overlap on the GPU
+ * race. With out_device NULL only *len (the block size) is written. */
+int mbg_material_constants_noalloc(
+    const char* algo,
+    const mbg_material* mat,
+    double timestep,
+    double* out_device,
+    size_t cap,
+    size_t* len,
+    void* stream);
+
 /* Offsets of the fields in mbg_material_constants' output for N levels:
  * writes name=offset pairs as text ("a=0\nb=1\n..."). */
 size_t mbg_material_layout(

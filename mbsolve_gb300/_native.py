@@ -79,6 +79,9 @@ def load():
     L.mbg_material_constants.argtypes = [C.c_char_p, P(T.mbg_material),
                                          C.c_double, C.c_int, T.PD,
                                          C.c_size_t, P(C.c_size_t)]
+    L.mbg_material_constants_noalloc.argtypes = [
+        C.c_char_p, P(T.mbg_material), C.c_double, C.c_void_p, C.c_size_t,
+        P(C.c_size_t), C.c_void_p]
     L.mbg_material_layout.restype = C.c_size_t
     L.mbg_material_layout.argtypes = [C.c_char_p, C.c_uint32, C.c_char_p,
                                       C.c_size_t]

@@ -42,6 +42,11 @@ void fill_grid(const mbg::run_setup& r, mbg_grid* g)
 
 }  // namespace
 
+namespace mbg {
+// lets entry points defined in other files report through mbg_last_error()
+void set_last_error(const char* msg) { g_last_error = msg; }
+}  // namespace mbg
+
 struct mbg_solver {
     std::unique_ptr<mbg::engine> eng;
 };
