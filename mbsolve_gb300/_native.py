@@ -85,6 +85,18 @@ def load():
     L.mbg_material_layout.restype = C.c_size_t
     L.mbg_material_layout.argtypes = [C.c_char_p, C.c_uint32, C.c_char_p,
                                       C.c_size_t]
+    # include/mbsolve_fno.h
+    vp, i32, i64, f32, f64 = C.c_void_p, C.c_int32, C.c_int64, C.c_float, C.c_double
+    L.mbg_fno_gemm.argtypes = [P(T.mbg_gemm_desc), vp]
+    L.mbg_fno_mode_blocks.argtypes = [vp, vp, i32, i32, vp, vp]
+    L.mbg_fno_cast_bf16.argtypes = [vp, vp, i64, vp]
+    L.mbg_fno_colsum.argtypes = [vp, i64, i32, i64, vp, vp]
+    L.mbg_fno_mse.argtypes = [vp, vp, i64, vp, vp, vp]
+    L.mbg_fno_adam.argtypes = [vp, vp, vp, vp, i64, f32, f32, f32, f32, f32,
+                               i32, vp]
+    L.mbg_fno_envelope.argtypes = [vp, i32, i32, i64, f64, f64, f64, i32,
+                                   f64, f64, vp, vp]
+    L.mbg_fno_status.argtypes = [P(C.c_uint32)]
     _lib = L
     return L
 

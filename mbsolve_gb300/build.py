@@ -33,6 +33,7 @@ def _headers():
     hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC)
           if f.endswith((".cuh", ".hpp", ".h"))]
     hs.append(os.path.join(HERE, "..", "include", "mbsolve_gb300.h"))
+    hs.append(os.path.join(HERE, "..", "include", "mbsolve_fno.h"))
     return hs
 
 

@@ -145,3 +145,40 @@ class PodBundle:
     def hold(self, obj):
         self.keep.append(obj)
         return obj
+
+
+# ---- include/mbsolve_fno.h
+MBG_F32, MBG_BF16 = 0, 1
+MBG_GEMM_STORE, MBG_GEMM_ACCUM, MBG_GEMM_ATOMIC = 0, 1, 2
+MBG_ACT_NONE, MBG_ACT_GELU, MBG_ACT_GELU_BWD = 0, 1, 2
+
+
+class mbg_gemm_segment(C.Structure):
+    _fields_ = [
+        ("a", C.c_void_p),
+        ("b", C.c_void_p),
+        ("a_sm", C.c_int64), ("a_sk", C.c_int64), ("a_sz", C.c_int64),
+        ("b_sn", C.c_int64), ("b_sk", C.c_int64), ("b_sz", C.c_int64),
+        ("k", C.c_int32),
+        ("a_type", C.c_int32),
+        ("b_type", C.c_int32),
+        ("negate", C.c_int32),
+    ]
+
+
+class mbg_gemm_desc(C.Structure):
+    _fields_ = [
+        ("m", C.c_int32), ("n", C.c_int32), ("batch", C.c_int32),
+        ("nseg", C.c_int32),
+        ("seg", mbg_gemm_segment * 3),
+        ("c", C.c_void_p),
+        ("c_sm", C.c_int64), ("c_sn", C.c_int64), ("c_sz", C.c_int64),
+        ("c_type", C.c_int32),
+        ("mode", C.c_int32),
+        ("act", C.c_int32),
+        ("split_k", C.c_int32),
+        ("alpha", C.c_float),
+        ("bias", C.c_void_p),
+        ("pre", C.c_void_p),
+        ("gate", C.c_void_p),
+    ]

@@ -10,6 +10,11 @@ namespace mbg {
 template<typename T, int ALGO, int LEV, int C, int NT>
 void launch_step(const kparams<T>& p, unsigned grid, size_t smem, cudaStream_t s)
 {
+    // 4 and more levels: uniform tiles stage the padded copy (cvr_pad)
+    if constexpr (ALGO == 1 && density_len<ALGO, LEV>::value >= 15) {
+        const size_t pad = (size_t) cvr_pad<T, density_len<ALGO, LEV>::value>::len * sizeof(T);
+        if (smem < pad) smem = pad;
+    }
     step_kernel<T, ALGO, LEV, C, NT><<<grid, NT, smem, s>>>(p);
 }
 

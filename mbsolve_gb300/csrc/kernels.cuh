@@ -29,6 +29,8 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "precompute.cuh"
 
@@ -175,10 +177,23 @@ __device__ __forceinline__ void store_cells(
         if (l0 + j >= lo && l0 + j < hi) dst[g0 + j] = r[j];
 }
 
+// An opaque copy of a pointer: loads through it can neither be hoisted out
+// of the time loop nor shared between the two passes of one step. For 4 and
+// more levels the compiler would otherwise keep the V x V coefficients live
+// across steps and spill them to local memory.
+template<typename T>
+__device__ __forceinline__ const T* opaque_ptr(const T* p)
+{
+    const T* r;
+    asm volatile("mov.b64 %0, %1;" : "=l"(r) : "l"(p));
+    return r;
+}
+
 // Coefficients of the coherence-vector update, read through a pointer
 // (shared memory for uniform tiles, global memory otherwise).
 template<typename T, int V>
 struct cvr_coef {
+    static constexpr bool VEC = false;
     static constexpr int KP = V / 2;
     static constexpr int oBd = pre::FDTD_END;
     static constexpr int oBdl = oBd + V * V;
@@ -192,7 +207,131 @@ struct cvr_coef {
     __device__ __forceinline__ T g(int i) const { return base[og + i]; }
     __device__ __forceinline__ T th(int k) const { return base[oth + k]; }
     __device__ __forceinline__ T p0() const { return base[5]; }
+    // the coefficients of one pass (see opaque_ptr)
+    __device__ __forceinline__ cvr_coef pass() const
+    {
+        if constexpr (V >= 15)
+            return cvr_coef{ opaque_ptr(base) };
+        else
+            return *this;
+    }
 };
+
+// Compile-time loop: f(integral_constant<int, i>) for i in [B, E). Keeps
+// every array index a constant so per-point vectors stay in registers
+// (plain unrolled nested loops of 35 x 35 are not always fully unrolled).
+template<int B, int E, class F>
+__device__ __forceinline__ void static_for(F&& f)
+{
+    if constexpr (B < E) {
+        f(std::integral_constant<int, B>{});
+        static_for<B + 1, E>(f);
+    }
+}
+
+// Shared-memory copy of a material's coherence-vector coefficients for 4 and
+// more levels (V >= 15): the rows of Bd and Bdl are padded with zeros to a
+// multiple of 16 bytes so that the updates read them with 128-bit loads
+// (with scalar loads the 35 x 35 products of 6 levels are bound by the
+// shared-memory load rate, one load per FMA). k, g and theta dt follow
+// unchanged; the FDTD head (indices < FDTD_END, p0 at 5) is the same.
+template<typename T, int V>
+struct cvr_pad {
+    static constexpr int W = 16 / (int) sizeof(T);  // reals per 16 bytes
+    static constexpr int VP = (V + W - 1) / W * W;
+    static constexpr int KP = V / 2;
+    static constexpr int oBd = pre::FDTD_END;       // 48 or 96 bytes: aligned
+    static constexpr int oBdl = oBd + V * VP;
+    static constexpr int ok = oBdl + V * VP;
+    static constexpr int og = ok + V;
+    static constexpr int oth = og + V;
+    static constexpr int len = oth + (KP > 0 ? KP : 1);
+    // index in the material block for index i of the padded copy, -1: zero
+    __device__ __forceinline__ static int source(int i)
+    {
+        const int bd = pre::FDTD_END, bdl = bd + V * V, k = bdl + V * V;
+        if (i < oBd) return i;
+        if (i < ok) {
+            const int t = i < oBdl ? i - oBd : i - oBdl;
+            const int r = t / VP, c = t % VP;
+            if (c >= V) return -1;
+            return (i < oBdl ? bd : bdl) + r * V + c;
+        }
+        return k + (i - ok);
+    }
+};
+
+// 16 bytes of shared memory at a shared-window address
+__device__ __forceinline__ void lds16(uint32_t a, float (&v)[4])
+{
+    asm("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3])
+        : "r"(a));
+}
+__device__ __forceinline__ void lds16(uint32_t a, double (&v)[2])
+{
+    asm("ld.shared.v2.f64 {%0, %1}, [%2];" : "=d"(v[0]), "=d"(v[1]) : "r"(a));
+}
+
+// Accessor of the padded copy. Loads go through a shared-window address that
+// is made opaque once per pass (see opaque_ptr).
+template<typename T, int V>
+struct cvr_coef_pad {
+    using Lp = cvr_pad<T, V>;
+    static constexpr bool VEC = true;
+    static constexpr int W = Lp::W;
+    uint32_t sbase;  // shared-window address of the copy
+    const T* base;
+    __device__ __forceinline__ T k(int i) const { return base[Lp::ok + i]; }
+    __device__ __forceinline__ T g(int i) const { return base[Lp::og + i]; }
+    __device__ __forceinline__ T th(int q) const { return base[Lp::oth + q]; }
+    __device__ __forceinline__ T p0() const { return base[5]; }
+    // W consecutive entries of row i of Bd (Bdl), from column W q
+    __device__ __forceinline__ void Bdv(int i, int q, T (&v)[W]) const
+    {
+        lds16(sbase + (uint32_t) ((Lp::oBd + i * Lp::VP + W * q) * (int) sizeof(T)), v);
+    }
+    __device__ __forceinline__ void Bdlv(int i, int q, T (&v)[W]) const
+    {
+        lds16(sbase + (uint32_t) ((Lp::oBdl + i * Lp::VP + W * q) * (int) sizeof(T)), v);
+    }
+    __device__ __forceinline__ cvr_coef_pad pass() const
+    {
+        uint32_t a;
+        asm volatile("mov.b32 %0, %1;" : "=r"(a) : "r"(sbase));
+        return cvr_coef_pad{ a, opaque_ptr(base) };
+    }
+};
+
+// s + sum_j Bd(I, j) x[j] (and sl + sum_j Bdl(I, j) x[j] when LO), with
+// vector loads where the accessor has them
+template<bool LO, int I, typename T, int V, class CF>
+__device__ __forceinline__ void row_dot(const CF& c, const T (&x)[V], T& s, T& sl)
+{
+    if constexpr (CF::VEC) {
+        constexpr int W = CF::W;
+        static_for<0, (V + W - 1) / W>([&](auto Q) {
+            constexpr int q = decltype(Q)::value;
+            T b[W], bl[W];
+            c.Bdv(I, q, b);
+            if constexpr (LO) c.Bdlv(I, q, bl);
+            static_for<0, W>([&](auto R) {
+                constexpr int r = decltype(R)::value;
+                constexpr int j = W * q + r;
+                if constexpr (j < V) {
+                    s = fma(b[r], x[j], s);
+                    if constexpr (LO) sl = fma(bl[r], x[j], sl);
+                }
+            });
+        });
+    } else {
+        static_for<0, V>([&](auto J) {
+            constexpr int j = decltype(J)::value;
+            s = fma(c.Bd(I, j), x[j], s);
+            if constexpr (LO) sl = fma(c.Bdl(I, j), x[j], sl);
+        });
+    }
+}
 
 // Coherence-vector update in the plane basis (see precompute.cuh):
 // w = u + (Bd u + k); rotate each plane by theta_k dt e; u = w + (Bd w + k);
@@ -201,30 +340,30 @@ template<typename T, int V, class CF>
 __device__ __forceinline__ void cvr_update(T (&u)[V], T e, T& pout, const CF& cf)
 {
     T w[V];
-#pragma unroll
-    for (int i = 0; i < V; i++) {
-        T s = cf.k(i);
-#pragma unroll
-        for (int j = 0; j < V; j++) s = fma(cf.Bd(i, j), u[j], s);
+    const auto c1 = cf.pass();
+    static_for<0, V>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        T s = c1.k(i), sl = T(0);
+        row_dot<false, i>(c1, u, s, sl);
         w[i] = u[i] + s;
-    }
-#pragma unroll
-    for (int k = 0; k < V / 2; k++) {
+    });
+    static_for<0, V / 2>([&](auto K) {
+        constexpr int k = decltype(K)::value;
         T sn, s2;
-        rot_coeffs<T>(cf.th(k) * e, sn, s2);
+        rot_coeffs<T>(c1.th(k) * e, sn, s2);
         T a = w[2 * k], b = w[2 * k + 1];
         w[2 * k] = a - fma(s2, a, sn * b);
         w[2 * k + 1] = b + fma(sn, a, -s2 * b);
-    }
-    T pp = cf.p0();
-#pragma unroll
-    for (int i = 0; i < V; i++) {
-        T s = cf.k(i);
-#pragma unroll
-        for (int j = 0; j < V; j++) s = fma(cf.Bd(i, j), w[j], s);
+    });
+    const auto c2 = cf.pass();
+    T pp = c2.p0();
+    static_for<0, V>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        T s = c2.k(i), sl = T(0);
+        row_dot<false, i>(c2, w, s, sl);
         u[i] = w[i] + s;
-        pp = fma(cf.g(i), u[i], pp);
-    }
+        pp = fma(c2.g(i), u[i], pp);
+    });
     pout = pp;
 }
 
@@ -250,6 +389,7 @@ __device__ __forceinline__ void df_renorm(float& h, float& l)
 // Coefficients of the 2-level update held in registers (uniform tiles).
 template<typename T, int V>
 struct cvr_coef_reg {
+    static constexpr bool VEC = false;
     T bd[V * V], bdl[V * V], kk[V], gg[V], thv[V / 2 > 0 ? V / 2 : 1], pz;
     __device__ __forceinline__ explicit cvr_coef_reg(const T* base)
     {
@@ -274,6 +414,7 @@ struct cvr_coef_reg {
     __device__ __forceinline__ T g(int i) const { return gg[i]; }
     __device__ __forceinline__ T th(int q) const { return thv[q]; }
     __device__ __forceinline__ T p0() const { return pz; }
+    __device__ __forceinline__ const cvr_coef_reg& pass() const { return *this; }  // stays in registers
 };
 
 // The same update in FP32 with u = uh + ul: the corrections are computed in
@@ -284,43 +425,37 @@ template<int V, class CF>
 __device__ __forceinline__ void cvr_update_df(float (&uh)[V], float (&ul)[V], float e, float& pout, const CF& cf)
 {
     float wh[V], wl[V];
-#pragma unroll
-    for (int i = 0; i < V; i++) {
-        float c = cf.k(i), cl = 0.0f;
-#pragma unroll
-        for (int j = 0; j < V; j++) {
-            c = fmaf(cf.Bd(i, j), uh[j], c);
-            cl = fmaf(cf.Bdl(i, j), uh[j], cl);
-        }
+    const auto c1 = cf.pass();
+    static_for<0, V>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        float c = c1.k(i), cl = 0.0f;
+        row_dot<true, i>(c1, uh, c, cl);
         wh[i] = uh[i];
         wl[i] = ul[i];
         df_acc(wh[i], wl[i], c, cl);
-    }
-#pragma unroll
-    for (int k = 0; k < V / 2; k++) {
+    });
+    static_for<0, V / 2>([&](auto K) {
+        constexpr int k = decltype(K)::value;
         float sn, s2;
-        rot_coeffs<float>(cf.th(k) * e, sn, s2);
+        rot_coeffs<float>(c1.th(k) * e, sn, s2);
         const float a = wh[2 * k], b = wh[2 * k + 1];
         const float da = -fmaf(s2, a, sn * b);
         const float db = fmaf(sn, a, -s2 * b);
         df_acc(wh[2 * k], wl[2 * k], da, 0.0f);
         df_acc(wh[2 * k + 1], wl[2 * k + 1], db, 0.0f);
-    }
-    float pp = cf.p0();
-#pragma unroll
-    for (int i = 0; i < V; i++) {
-        float c = cf.k(i), cl = 0.0f;
-#pragma unroll
-        for (int j = 0; j < V; j++) {
-            c = fmaf(cf.Bd(i, j), wh[j], c);
-            cl = fmaf(cf.Bdl(i, j), wh[j], cl);
-        }
+    });
+    const auto c2 = cf.pass();
+    float pp = c2.p0();
+    static_for<0, V>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        float c = c2.k(i), cl = 0.0f;
+        row_dot<true, i>(c2, wh, c, cl);
         uh[i] = wh[i];
         ul[i] = wl[i];
         df_acc(uh[i], ul[i], c, cl);
         df_renorm(uh[i], ul[i]);
-        pp = fmaf(cf.g(i), uh[i], fmaf(cf.g(i), ul[i], pp));
-    }
+        pp = fmaf(c2.g(i), uh[i], fmaf(c2.g(i), ul[i], pp));
+    });
     pout = pp;
 }
 

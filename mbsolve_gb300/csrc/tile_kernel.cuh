@@ -57,8 +57,10 @@ __device__ __forceinline__ void tile_steps(
     constexpr bool DF = sizeof(T) == 4;
     constexpr int D = density_len<ALGO, LEV>::value;
     constexpr int NW = NT / 32;
-    // 2-level coefficients live in registers on uniform tiles
+    // 2-level coefficients live in registers on uniform tiles; for 4 and more
+    // levels uniform tiles hold the padded copy of cvr_pad in shared memory
     constexpr bool REGCOEF = UNIFORM && ALGO == 1 && D == 3;
+    constexpr bool PADC = UNIFORM && ALGO == 1 && D >= 15;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int64_t nx = rd.n_x;
@@ -166,6 +168,12 @@ __device__ __forceinline__ void tile_steps(
                             cvr_update_df<D>(R[j], Rl[j], e, P[j], creg);
                         else
                             cvr_update<T, D>(R[j], e, P[j], creg);
+                    } else if constexpr (PADC) {
+                        const cvr_coef_pad<T, D> cf{ (uint32_t) __cvta_generic_to_shared(sh_coef), sh_coef };
+                        if constexpr (DF)
+                            cvr_update_df<D>(R[j], Rl[j], e, P[j], cf);
+                        else
+                            cvr_update<T, D>(R[j], e, P[j], cf);
                     } else {
                         cvr_coef<T, D> cf{ cb };
                         if constexpr (DF)
@@ -201,7 +209,10 @@ __device__ __forceinline__ void tile_steps(
                         case 2: v = hv; break;
                         case 4: v = R[j][1] - R[j][0]; break;
                         case 3:
-                            if (rc.row_idx == rc.col_idx && rc.row_idx < (uint32_t) LEV) v = R[j][rc.row_idx];
+                            // constant indices keep R in registers
+#pragma unroll
+                            for (int q = 0; q < LEV; q++)
+                                if (rc.row_idx == rc.col_idx && rc.row_idx == (uint32_t) q) v = R[j][q];
                             break;
                         }
                     } else {
@@ -209,7 +220,9 @@ __device__ __forceinline__ void tile_steps(
                         T u[DDv];
 #pragma unroll
                         for (int q = 0; q < DDv; q++) u[q] = DF ? R[j][q] + Rl[j][q] : R[j][q];
-                        v = cvr_record_value<T, D>(rc, ev, hv, P[j], u, block(j), LEV);
+                        // the padded shared copy lacks the record rows
+                        const T* rb = PADC ? p.mc + (uint64_t) M[j] * p.mstride : block(j);
+                        v = cvr_record_value<T, D>(rc, ev, hv, P[j], u, rb, LEV);
                     }
                     const uint64_t row = rc.ratio == 1.0 ? n : (uint64_t) floor(rc.ratio * (double) n);
                     if (row < rc.rows) {
@@ -317,7 +330,15 @@ __global__ void __launch_bounds__(NT) step_kernel(const kparams<T> p)
     const bool uniform = td.uniform_mat >= 0;
     if (uniform) {
         const T* src = p.mc + (uint64_t) td.uniform_mat * p.mstride;
-        for (int i = threadIdx.x; i < (int) p.mstage; i += NT) sh_coef[i] = src[i];
+        if constexpr (ALGO == 1 && D >= 15) {
+            using Lp = cvr_pad<T, D>;
+            for (int i = threadIdx.x; i < Lp::len; i += NT) {
+                const int q = Lp::source(i);
+                sh_coef[i] = q >= 0 ? src[q] : T(0);
+            }
+        } else {
+            for (int i = threadIdx.x; i < (int) p.mstage; i += NT) sh_coef[i] = src[i];
+        }
     }
     __syncthreads();
 

@@ -1,0 +1,304 @@
+"""Fourier-neural-operator surrogate of the Maxwell-Bloch solver.
+
+Maps an input pulse envelope (S samples) and medium parameters to the
+transmitted envelope at the output facet, to prescreen parameter sweeps; the
+solver stays the fallback and the judge of its error. The network is a 1-D
+Fourier neural operator (Li et al., ICLR 2021): a lifting layer, L Fourier
+layers (truncated real DFT to Mo modes, complex mode mixing, inverse DFT,
+plus a pointwise channel mix; GELU between layers) and a two-layer
+projection. It has no counterpart in the reference.
+
+All arithmetic runs in this package's kernels (include/mbsolve_fno.h): every
+product, forward and backward, is one launch of the tcgen05 tensor-core
+GEMM (BF16 operands, FP32 accumulation), fused with its bias / GELU /
+GELU-derivative epilogue; the truncated DFT and its inverse are products
+with fixed BF16 bases. Master weights, gradients and Adam moments are FP32
+in one flat buffer each. torch provides device memory and the stream only.
+
+Layouts (row-major, element strides): activations v_l [B, S, W] BF16,
+pre-activations [B, S, W] FP32, spectra Vh [B, W, 2 Mo] FP32 (Re modes then
+Im modes), mixed spectra Y [B, Mo, 2 W] FP32, mode blocks [Mo, 2W, 2W] BF16.
+"""
+import math
+
+import numpy as np
+import torch
+
+from . import capi_types as T
+from . import surrogate_kernels as K
+from .surrogate_kernels import Seg
+
+
+class Shapes:
+    """Network sizes: samples S, width W, modes Mo, layers L, input
+    features F (envelope, medium parameters, grid coordinate), projection
+    width Hq."""
+
+    def __init__(self, S=1024, W=64, Mo=32, L=4, F=8, Hq=128):
+        self.S, self.W, self.Mo, self.L, self.F, self.Hq = S, W, Mo, L, F, Hq
+        if W % 8 or Mo % 8:
+            raise ValueError("width and modes must be multiples of 8")
+        if 2 * Mo > S // 2 + 1:
+            raise ValueError("too many modes for S samples")
+
+    def param_spec(self):
+        """(name, shape) in the order of the flat parameter vector."""
+        W, Mo, F, Hq = self.W, self.Mo, self.F, self.Hq
+        spec = [("P", (W, F)), ("bp", (W,))]
+        for l in range(self.L):
+            spec += [("wr%d" % l, (Mo, W, W)), ("wi%d" % l, (Mo, W, W)),
+                     ("W%d" % l, (W, W)), ("bw%d" % l, (W,))]
+        spec += [("Q1", (Hq, W)), ("bq1", (Hq,)), ("q2", (Hq,)),
+                 ("bq2", (1,))]
+        return spec
+
+    def num_params(self):
+        return sum(int(np.prod(s)) for _, s in self.param_spec())
+
+
+def dft_bases(S, Mo):
+    """Truncated real DFT and its inverse (float64):
+    F [2Mo, S] = [cos(2 pi m s / S); -sin(2 pi m s / S)] / S and
+    G [S, 2Mo] = [c_m cos, -c_m sin] with c_0 = 1, c_m = 2, so that
+    G F x is x low-passed to its first Mo harmonics."""
+    s = np.arange(S)[None, :]
+    m = np.arange(Mo)[:, None]
+    ang = 2.0 * math.pi * m * s / S
+    F = np.concatenate([np.cos(ang), -np.sin(ang)], axis=0) / S
+    c = np.where(np.arange(Mo) == 0, 1.0, 2.0)[None, :]
+    G = np.concatenate([c * np.cos(ang.T), -c * np.sin(ang.T)], axis=1)
+    return np.ascontiguousarray(F), np.ascontiguousarray(G)
+
+
+def init_params(sh, seed=0):
+    """Seeded initialisation: linear layers uniform in +-1/sqrt(fan_in),
+    spectral weights uniform in [0, 1) / W^2."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for name, shape in sh.param_spec():
+        if name.startswith(("wr", "wi")):
+            a = rng.uniform(0.0, 1.0, size=shape) / (sh.W * sh.W)
+        elif name in ("P", "Q1") or (name[0] == "W" and name[1:].isdigit()):
+            a = rng.uniform(-1, 1, size=shape) / math.sqrt(shape[1])
+        elif name == "q2":
+            a = rng.uniform(-1, 1, size=shape) / math.sqrt(sh.Hq)
+        else:
+            fan = {"bp": sh.F, "bq1": sh.W, "bq2": sh.Hq}.get(name, sh.W)
+            a = rng.uniform(-1, 1, size=shape) / math.sqrt(fan)
+        out.append(a.ravel())
+    return np.concatenate(out)
+
+
+class FNO:
+    """The network on one GPU. forward(X) -> y; backward(dy) fills grad;
+    train_step(X, t) runs forward, loss, backward and one Adam step."""
+
+    def __init__(self, shapes=None, seed=0, device="cuda"):
+        self.sh = sh = shapes or Shapes()
+        self.dev = torch.device(device)
+        n = sh.num_params()
+        self.theta = torch.tensor(init_params(sh, seed), dtype=torch.float32,
+                                  device=self.dev)
+        self.grad = torch.zeros(n, dtype=torch.float32, device=self.dev)
+        self.m1 = torch.zeros_like(self.grad)
+        self.m2 = torch.zeros_like(self.grad)
+        self.step_count = 0
+        self.p = self._views(self.theta)
+        self.g = self._views(self.grad)
+        F, G = dft_bases(sh.S, sh.Mo)
+        self.F = torch.tensor(F, dtype=torch.float32).to(torch.bfloat16).to(self.dev).contiguous()
+        self.G = torch.tensor(G, dtype=torch.float32).to(torch.bfloat16).to(self.dev).contiguous()
+        self.blk = [torch.empty(sh.Mo * 4 * sh.W * sh.W, dtype=torch.bfloat16,
+                                device=self.dev) for _ in range(sh.L)]
+        self._bufs = {}
+        self._blk_valid = False
+
+    # ------------------------------------------------------------ helpers
+    def _views(self, flat):
+        out, o = {}, 0
+        for name, shape in self.sh.param_spec():
+            k = int(np.prod(shape))
+            out[name] = flat[o:o + k]
+            o += k
+        return out
+
+    def load_params(self, theta):
+        self.theta.copy_(torch.as_tensor(theta, dtype=torch.float32))
+        self._blk_valid = False
+
+    def _buffers(self, B):
+        if B in self._bufs:
+            return self._bufs[B]
+        sh, d = self.sh, self.dev
+        S, W, Mo, L, Hq = sh.S, sh.W, sh.Mo, sh.L, sh.Hq
+        f32, b16 = torch.float32, torch.bfloat16
+        b = dict(
+            v=[torch.empty(B * S * W, dtype=b16, device=d) for _ in range(L + 1)],
+            pre=[torch.empty(B * S * W, dtype=f32, device=d) for _ in range(L - 1)],
+            Vh=[torch.empty(B * W * 2 * Mo, dtype=f32, device=d) for _ in range(L)],
+            Y=torch.empty(B * Mo * 2 * W, dtype=f32, device=d),
+            ph=torch.empty(B * S * Hq, dtype=f32, device=d),
+            h=torch.empty(B * S * Hq, dtype=b16, device=d),
+            y=torch.empty(B * S, dtype=f32, device=d),
+            dy=torch.empty(B * S, dtype=f32, device=d),
+            dh=torch.empty(B * S * Hq, dtype=f32, device=d),
+            dpre=[torch.empty(B * S * W, dtype=f32, device=d) for _ in range(2)],
+            dY=torch.empty(B * 2 * Mo * W, dtype=f32, device=d),
+            dVh=torch.empty(B * W * 2 * Mo, dtype=f32, device=d),
+            loss=torch.zeros(1, dtype=f32, device=d),
+        )
+        self._bufs[B] = b
+        return b
+
+    def _mode_blocks(self):
+        for l in range(self.sh.L):
+            K.mode_blocks(self.p["wr%d" % l].view(self.sh.Mo, self.sh.W, self.sh.W),
+                          self.p["wi%d" % l], self.blk[l])
+        self._blk_valid = True
+
+    @staticmethod
+    def _split(rows):
+        """K splits of a weight-gradient product over `rows` rows."""
+        return max(1, min(152, rows // 512))
+
+    # ------------------------------------------------------------ forward
+    def forward(self, X):
+        """X: FP32 CUDA tensor [B, S, F]. Returns y [B, S] (FP32, a view of
+        an internal buffer: copy it to keep it past the next call)."""
+        sh = self.sh
+        S, W, Mo, L, Fi, Hq = sh.S, sh.W, sh.Mo, sh.L, sh.F, sh.Hq
+        B = X.shape[0]
+        if tuple(X.shape) != (B, S, Fi) or X.dtype != torch.float32:
+            raise ValueError("X must be FP32 [B, %d, %d]" % (S, Fi))
+        X = X.contiguous()
+        b = self._buffers(B)
+        p = self.p
+        if not self._blk_valid:
+            self._mode_blocks()
+        self._X = X
+        # lifting: v0 = X P^T + bp
+        K.gemm(B * S, W, [Seg(X, 0, Fi, 1, 0, p["P"], 0, Fi, 1, 0, Fi)],
+               b["v"][0], 0, W, 1, bias=p["bp"])
+        for l in range(L):
+            v, vh = b["v"][l], b["Vh"][l]
+            # truncated DFT: Vh[b, c, m'] = sum_s F[m', s] v[b, s, c]
+            K.gemm(W, 2 * Mo, [Seg(v, 0, 1, W, S * W, self.F, 0, S, 1, 0, S)],
+                   vh, 0, 2 * Mo, 1, W * 2 * Mo, batch=B)
+            # mode mixing, per mode m: Y[b, m, :] = blk[m] [Re; Im]
+            blk = self.blk[l]
+            K.gemm(B, 2 * W,
+                   [Seg(vh, 0, W * 2 * Mo, 2 * Mo, 1, blk, 0, 2 * W, 1, 4 * W * W, W),
+                    Seg(vh, Mo, W * 2 * Mo, 2 * Mo, 1, blk, W, 2 * W, 1, 4 * W * W, W)],
+                   b["Y"], 0, Mo * 2 * W, 1, 2 * W, batch=Mo)
+            # inverse DFT + pointwise path + bias (+ GELU), per sample
+            last = l == L - 1
+            K.gemm(S, W,
+                   [Seg(self.G, 0, 2 * Mo, 1, 0, b["Y"], 0, 1, 2 * W, Mo * 2 * W, Mo),
+                    Seg(self.G, Mo, 2 * Mo, 1, 0, b["Y"], W, 1, 2 * W, Mo * 2 * W, Mo),
+                    Seg(v, 0, W, 1, S * W, p["W%d" % l], 0, W, 1, 0, W)],
+                   b["v"][l + 1], 0, W, 1, S * W, batch=B, bias=p["bw%d" % l],
+                   act=T.MBG_ACT_NONE if last else T.MBG_ACT_GELU,
+                   pre=None if last else b["pre"][l])
+        # projection
+        K.gemm(B * S, Hq, [Seg(b["v"][L], 0, W, 1, 0, p["Q1"], 0, W, 1, 0, W)],
+               b["h"], 0, Hq, 1, bias=p["bq1"], act=T.MBG_ACT_GELU, pre=b["ph"])
+        K.gemm(B * S, 1, [Seg(b["h"], 0, Hq, 1, 0, p["q2"], 0, 0, 1, 0, Hq)],
+               b["y"], 0, 1, 1, bias=p["bq2"])
+        return b["y"].view(B, S)
+
+    # ------------------------------------------------------------ backward
+    def backward(self, dy=None):
+        """Gradient of the loss into self.grad (zeroed first). dy: FP32
+        [B, S] gradient of the loss w.r.t. the last forward's output, or
+        None when loss() already wrote it."""
+        sh = self.sh
+        S, W, Mo, L, Fi, Hq = sh.S, sh.W, sh.Mo, sh.L, sh.F, sh.Hq
+        X = self._X
+        B = X.shape[0]
+        if B % 8:
+            raise ValueError("backward needs a batch that is a multiple of 8")
+        b = self._buffers(B)
+        p, g = self.p, self.g
+        if dy is not None:
+            b["dy"].copy_(dy.reshape(-1))
+        dyb = b["dy"]
+        R = B * S
+        self.grad.zero_()
+        ATOM = T.MBG_GEMM_ATOMIC
+        # output layer
+        K.gemm(Hq, 1, [Seg(b["h"], 0, 1, Hq, 0, dyb, 0, 0, 1, 0, R)],
+               g["q2"], 0, 1, 1, mode=ATOM, split_k=self._split(R))
+        K.colsum(dyb, R, 1, 1, g["bq2"])
+        K.gemm(R, Hq, [Seg(dyb, 0, 1, 1, 0, p["q2"], 0, 1, 1, 0, 1)],
+               b["dh"], 0, Hq, 1, act=T.MBG_ACT_GELU_BWD, gate=b["ph"])
+        K.gemm(Hq, W, [Seg(b["dh"], 0, 1, Hq, 0, b["v"][L], 0, 1, W, 0, R)],
+               g["Q1"], 0, W, 1, mode=ATOM, split_k=self._split(R))
+        K.colsum(b["dh"], R, Hq, Hq, g["bq1"])
+        cur = 0
+        K.gemm(R, W, [Seg(b["dh"], 0, Hq, 1, 0, p["Q1"], 0, 1, W, 0, Hq)],
+               b["dpre"][cur], 0, W, 1)
+        for l in range(L - 1, -1, -1):
+            dpre = b["dpre"][cur]
+            vh, blk = b["Vh"][l], self.blk[l]
+            K.gemm(W, W, [Seg(dpre, 0, 1, W, 0, b["v"][l], 0, 1, W, 0, R)],
+                   g["W%d" % l], 0, W, 1, mode=ATOM, split_k=self._split(R))
+            K.colsum(dpre, R, W, W, g["bw%d" % l])
+            # dY[b, m', o] = sum_s G[s, m'] dpre[b, s, o]
+            K.gemm(2 * Mo, W, [Seg(self.G, 0, 1, 2 * Mo, 0, dpre, 0, 1, W, S * W, S)],
+                   b["dY"], 0, W, 1, 2 * Mo * W, batch=B)
+            dY = b["dY"]
+            a_re = dict(a_sm=1, a_sk=2 * Mo * W, a_sz=W)
+            b_v = dict(b_sn=2 * Mo, b_sk=W * 2 * Mo, b_sz=1)
+
+            def sg(a_off, b_off, neg=False):
+                return Seg(dY, a_off, a_re["a_sm"], a_re["a_sk"], a_re["a_sz"],
+                           vh, b_off, b_v["b_sn"], b_v["b_sk"], b_v["b_sz"], B,
+                           negate=neg)
+            # spectral weights, per mode
+            K.gemm(W, W, [sg(0, 0), sg(Mo * W, Mo)],
+                   g["wr%d" % l], 0, 1, W, W * W, batch=Mo)
+            K.gemm(W, W, [sg(0, Mo, True), sg(Mo * W, 0)],
+                   g["wi%d" % l], 0, 1, W, W * W, batch=Mo)
+            # spectra: dVh = blk^T dY, Re and Im halves, per mode
+            for half in range(2):
+                K.gemm(B, W,
+                       [Seg(dY, 0, 2 * Mo * W, 1, W, blk, half * W, 1, 2 * W, 4 * W * W, W),
+                        Seg(dY, Mo * W, 2 * Mo * W, 1, W, blk, 2 * W * W + half * W, 1, 2 * W,
+                            4 * W * W, W)],
+                       b["dVh"], half * Mo, W * 2 * Mo, 2 * Mo, 1, batch=Mo)
+            # activations: dv = F^T dVh + dpre W_l, then GELU'
+            nxt = 1 - cur
+            K.gemm(S, W,
+                   [Seg(self.F, 0, 1, S, 0, b["dVh"], 0, 2 * Mo, 1, W * 2 * Mo, 2 * Mo),
+                    Seg(dpre, 0, W, 1, S * W, p["W%d" % l], 0, 1, W, 0, W)],
+                   b["dpre"][nxt], 0, W, 1, S * W, batch=B,
+                   act=T.MBG_ACT_GELU_BWD if l > 0 else T.MBG_ACT_NONE,
+                   gate=b["pre"][l - 1] if l > 0 else None)
+            cur = nxt
+        dv0 = b["dpre"][cur]
+        K.gemm(W, Fi, [Seg(dv0, 0, 1, W, 0, X, 0, 1, Fi, 0, R)],
+               g["P"], 0, Fi, 1, mode=ATOM, split_k=self._split(R))
+        K.colsum(dv0, R, W, W, g["bp"])
+
+    def loss(self, target):
+        """Mean squared error of the last forward against target [B, S];
+        writes the output gradient for backward(). Returns the loss as a
+        one-element CUDA tensor (no synchronisation)."""
+        B = self._X.shape[0]
+        b = self._buffers(B)
+        b["loss"].zero_()
+        K.mse(b["y"], target.reshape(-1), b["dy"], b["loss"])
+        return b["loss"]
+
+    def adam(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=0.0):
+        self.step_count += 1
+        K.adam(self.theta, self.grad, self.m1, self.m2, lr, beta1, beta2, eps,
+               weight_decay, self.step_count)
+        self._blk_valid = False
+
+    def train_step(self, X, target, lr=1e-3, weight_decay=0.0):
+        self.forward(X)
+        loss = self.loss(target)
+        self.backward()
+        self.adam(lr=lr, weight_decay=weight_decay)
+        return loss

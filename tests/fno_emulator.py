@@ -1,0 +1,82 @@
+"""CPU model of the surrogate kernels' semantics (include/mbsolve_fno.h),
+for tests of the host-side product plan without a GPU: the same arguments
+surrogate_kernels receives, evaluated with torch on the CPU (BF16 operand
+rounding, FP32 stores, the same epilogues). Test infrastructure only."""
+import math
+
+import torch
+
+
+def _view(t, off, size, stride):
+    # element offsets are relative to the tensor (a view into a flat buffer)
+    return torch.as_strided(t, size, stride, t.storage_offset() + int(off))
+
+
+def _bf(x):
+    return x.to(torch.bfloat16).to(torch.float64)
+
+
+def gemm(m, n, segs, c, c_off, c_sm, c_sn, c_sz=0, batch=1, mode=0, act=0,
+         alpha=1.0, bias=None, pre=None, gate=None, split_k=1):
+    acc = torch.zeros(batch, m, n, dtype=torch.float64)
+    for s in segs:
+        A = _bf(_view(s.a, s.a_off, (batch, m, s.k), (s.a_sz, s.a_sm, s.a_sk)))
+        B = _bf(_view(s.b, s.b_off, (batch, n, s.k), (s.b_sz, s.b_sn, s.b_sk)))
+        p = A @ B.transpose(1, 2)
+        acc = acc - p if s.negate else acc + p
+    # FP32 accumulator
+    v = (alpha * acc.to(torch.float32).to(torch.float64))
+    C = _view(c, c_off, (batch, m, n), (c_sz, c_sm, c_sn))
+    if mode == 2:
+        C.copy_((C.to(torch.float64) + v).to(C.dtype))
+        return
+    if mode == 1:
+        v = v + C.to(torch.float64)
+    if bias is not None:
+        v = v + bias[:n].to(torch.float64)
+    v = v.to(torch.float32).to(torch.float64)
+    if pre is not None:
+        _view(pre, c_off, (batch, m, n), (c_sz, c_sm, c_sn)).copy_(v.to(torch.float32))
+    if act == 1:
+        v = 0.5 * v * (1.0 + torch.erf(v / math.sqrt(2.0)))
+    elif act == 2:
+        g = _view(gate, c_off, (batch, m, n), (c_sz, c_sm, c_sn)).to(torch.float64)
+        v = v * (0.5 * (1.0 + torch.erf(g / math.sqrt(2.0))) +
+                 g * torch.exp(-0.5 * g * g) / math.sqrt(2.0 * math.pi))
+    C.copy_(v.to(C.dtype))
+
+
+def mode_blocks(wr, wi, blk):
+    Mo, W = wr.shape[0], wr.shape[1]
+    r = wr.reshape(Mo, W, W).transpose(1, 2)
+    i = wi.reshape(Mo, W, W).transpose(1, 2)
+    top = torch.cat([r, -i], dim=2)
+    bot = torch.cat([i, r], dim=2)
+    blk.copy_(torch.cat([top, bot], dim=1).reshape(-1).to(blk.dtype))
+
+
+def colsum(x, rows, cols, row_stride, out):
+    v = _view(x, 0, (rows, cols), (row_stride, 1)).to(torch.float64).sum(0)
+    out[:cols] += v.to(torch.float32)
+
+
+def mse(y, t, grad, loss):
+    n = y.numel()
+    d = y.to(torch.float64) - t.to(torch.float64)
+    grad.copy_((2.0 * d / n).to(torch.float32))
+    loss += float((d * d).sum() / n)
+
+
+def adam(w, g, m, v, lr, beta1, beta2, eps, weight_decay, step):
+    m.mul_(beta1).add_((1 - beta1) * g)
+    v.mul_(beta2).add_((1 - beta2) * g * g)
+    mh = m / (1 - beta1 ** step)
+    vh = v / (1 - beta2 ** step)
+    w.sub_(lr * (mh / (vh.sqrt() + eps) + weight_decay * w))
+
+
+def install(monkeypatch):
+    """Route the surrogate module's kernel calls to this model."""
+    from mbsolve_gb300 import surrogate as S
+    for name in ("gemm", "mode_blocks", "colsum", "mse", "adam"):
+        monkeypatch.setattr(S.K, name, globals()[name])

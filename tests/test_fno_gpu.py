@@ -1,0 +1,135 @@
+"""The surrogate network on the GPU (mbsolve_gb300/surrogate.py) against the
+CPU oracle (oracle/fno_oracle.py): outputs, loss and every parameter
+gradient, at a small size and at the full size of the workload (1,024
+samples, width 64, 32 modes, 4 layers); the Adam step and the envelope
+kernel against their formulas; and training that fits."""
+import math
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import fno_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+# The GPU rounds the same operands to BF16 as the oracle's bf16 mode; what is
+# left is FP32 accumulation order and FP32 erf/exp (a few BF16 roundings land
+# on the other side). Relative L2 tolerances:
+TOL_Y = 5e-3
+TOL_GRAD = 2e-2
+
+
+@pytest.fixture(scope="module")
+def S(native):
+    from mbsolve_gb300 import surrogate
+    assert torch.cuda.is_available()
+    return surrogate
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, np.float64).ravel(), np.asarray(b, np.float64).ravel()
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+
+
+def test_param_layout_and_bases_match_oracle(S):
+    for args in [dict(S=128, W=16, Mo=8, L=2, F=8, Hq=32), {}]:
+        a, b = S.Shapes(**args), O.Shapes(**args)
+        assert a.param_spec() == b.param_spec()
+        Fa, Ga = S.dft_bases(a.S, a.Mo)
+        Fb, Gb = O.dft_bases(b.S, b.Mo)
+        np.testing.assert_allclose(Fa, Fb, atol=1e-15)
+        np.testing.assert_allclose(Ga, Gb, atol=1e-13)
+
+
+@pytest.mark.parametrize("args,B", [(dict(S=128, W=16, Mo=8, L=2, F=8, Hq=32), 8),
+                                    ({}, 8)])
+def test_forward_and_gradients_match_oracle(S, args, B):
+    sh = S.Shapes(**args)
+    net = S.FNO(sh, seed=3)
+    rng = np.random.default_rng(11)
+    X = rng.normal(size=(B, sh.S, sh.F)).astype(np.float32)
+    t = rng.normal(size=(B, sh.S)).astype(np.float32)
+    y = net.forward(torch.tensor(X, device="cuda")).clone()
+    loss = net.loss(torch.tensor(t, device="cuda")).item()
+    net.backward()
+    torch.cuda.synchronize()
+    from mbsolve_gb300 import surrogate_kernels as K
+    assert K.status() == 0
+    theta = net.theta.cpu().double().numpy()
+    osh = O.Shapes(**args)
+    ol, og, oy = O.forward_backward(osh, theta, X.astype(np.float64),
+                                    t.astype(np.float64), bf16=True)
+    assert _rel(y.cpu().numpy(), oy) < TOL_Y
+    assert abs(loss - ol) < TOL_Y * ol
+    g = net.grad.cpu().double().numpy()
+    gp, op = O.unflatten(osh, g), O.unflatten(osh, og)
+    for name, _ in osh.param_spec():
+        assert _rel(gp[name], op[name]) < TOL_GRAD, name
+
+
+def test_adam_step_formula(S):
+    from mbsolve_gb300 import surrogate_kernels as K
+    rng = np.random.default_rng(5)
+    n = 1000
+    w, g = rng.normal(size=n), rng.normal(size=n)
+    m, v = rng.normal(size=n) * 0.1, rng.uniform(0, 1, size=n)
+    tw, tg, tm, tv = (torch.tensor(a, dtype=torch.float32, device="cuda")
+                      for a in (w, g, m, v))
+    lr, b1, b2, eps, wd, step = 1e-3, 0.9, 0.999, 1e-8, 1e-2, 7
+    K.adam(tw, tg, tm, tv, lr, b1, b2, eps, wd, step)
+    m2 = b1 * m + (1 - b1) * g
+    v2 = b2 * v + (1 - b2) * g * g
+    mh, vh = m2 / (1 - b1 ** step), v2 / (1 - b2 ** step)
+    w2 = w - lr * (mh / (np.sqrt(vh) + eps) + wd * w)
+    np.testing.assert_allclose(tw.cpu().numpy(), w2, rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(tm.cpu().numpy(), m2, rtol=1e-5, atol=1e-7)
+
+
+def test_envelope_of_modulated_signal(S):
+    from mbsolve_gb300 import surrogate_kernels as K
+    f0, dt, rows = 5e12, 4e-15, 4000
+    t = np.arange(rows) * dt
+    env = np.exp(-((t - 8e-12) / 2e-12) ** 2) * 3.0
+    runs = np.stack([env * np.sin(2 * math.pi * f0 * t + ph)
+                     for ph in (0.0, 1.0, 2.5)])
+    e = torch.tensor(runs, dtype=torch.float64, device="cuda")
+    nout = 256
+    out = torch.empty(3, nout, dtype=torch.float32, device="cuda")
+    K.envelope(e, 0.0, dt, f0, nout, 0.0, rows * dt / nout, out)
+    tj = np.arange(nout) * rows * dt / nout
+    want = 3.0 * np.exp(-((tj - 8e-12) / 2e-12) ** 2)
+    inner = (tj > 1e-12) & (tj < 15e-12)
+    for r in range(3):
+        assert np.abs(out[r].cpu().numpy()[inner] - want[inner]).max() < 0.02 * 3.0
+
+
+def test_training_fits_a_pulse_operator(S):
+    """Learns y = delayed envelope scaled by a per-sample gain: the loss
+    falls by more than 20x."""
+    sh = S.Shapes(S=256, W=32, Mo=16, L=2, F=8, Hq=64)
+    net = S.FNO(sh, seed=1)
+    rng = np.random.default_rng(2)
+    B, N = 16, 256
+    s = np.arange(sh.S) / sh.S
+    c = rng.uniform(0.2, 0.6, size=N)
+    w = rng.uniform(0.03, 0.08, size=N)
+    gain = rng.uniform(0.5, 1.5, size=N)
+    env = np.exp(-((s[None, :] - c[:, None]) / w[:, None]) ** 2)
+    X = np.zeros((N, sh.S, sh.F), np.float32)
+    X[..., 0] = env
+    X[..., 1] = (gain[:, None] - 1.0) * 2.0
+    X[..., 7] = s[None, :]
+    tgt = gain[:, None] * np.exp(-((s[None, :] - c[:, None] - 0.1) / w[:, None]) ** 2)
+    Xg = torch.tensor(X, device="cuda")
+    Tg = torch.tensor(tgt, dtype=torch.float32, device="cuda")
+    first = None
+    for it in range(300):
+        i0 = (it * B) % N
+        loss = net.train_step(Xg[i0:i0 + B], Tg[i0:i0 + B], lr=3e-3)
+        if it == 0:
+            first = loss.item()
+    last = np.mean([net.train_step(Xg[i:i + B], Tg[i:i + B], lr=1e-3).item()
+                    for i in range(0, N, B)])
+    assert last < first / 20, (first, last)

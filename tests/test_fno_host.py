@@ -1,0 +1,84 @@
+"""Host logic of the surrogate without a GPU: the network's plan of strided
+products (operand offsets, strides, K segments, epilogues) evaluated by a
+CPU model of the kernels equals the CPU oracle's forward and backward pass;
+the prescreen feature builder and sweep sampling are deterministic."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import fno_oracle as O
+
+from tests import fno_emulator as E
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, np.float64).ravel(), np.asarray(b, np.float64).ravel()
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+
+
+@pytest.mark.parametrize("args", [dict(S=64, W=8, Mo=8, L=2, F=8, Hq=16),
+                                  dict(S=128, W=16, Mo=8, L=3, F=9, Hq=32)])
+def test_product_plan_equals_oracle(monkeypatch, args):
+    from mbsolve_gb300 import surrogate as S
+    E.install(monkeypatch)
+    sh = S.Shapes(**args)
+    net = S.FNO(sh, seed=4, device="cpu")
+    rng = np.random.default_rng(9)
+    B = 8
+    X = rng.normal(size=(B, sh.S, sh.F)).astype(np.float32)
+    t = rng.normal(size=(B, sh.S)).astype(np.float32)
+    y = net.forward(torch.tensor(X)).clone()
+    loss = net.loss(torch.tensor(t)).item()
+    net.backward()
+    theta = net.theta.double().numpy()
+    osh = O.Shapes(**args)
+    ol, og, oy = O.forward_backward(osh, theta, X.astype(np.float64),
+                                    t.astype(np.float64), bf16=True)
+    assert _rel(y.numpy(), oy) < 1e-3
+    assert abs(loss - ol) < 1e-3 * ol
+    gp = O.unflatten(osh, net.grad.double().numpy())
+    op = O.unflatten(osh, og)
+    for name, _ in osh.param_spec():
+        assert _rel(gp[name], op[name]) < 1e-2, name
+
+
+def test_training_step_moves_toward_lower_loss(monkeypatch):
+    from mbsolve_gb300 import surrogate as S
+    E.install(monkeypatch)
+    sh = S.Shapes(S=64, W=8, Mo=8, L=2, F=8, Hq=16)
+    net = S.FNO(sh, seed=1, device="cpu")
+    rng = np.random.default_rng(3)
+    X = torch.tensor(rng.normal(size=(8, sh.S, sh.F)).astype(np.float32))
+    t = torch.tensor(rng.normal(size=(8, sh.S)).astype(np.float32))
+    l0 = net.train_step(X, t, lr=1e-3).item()
+    for _ in range(20):
+        l1 = net.train_step(X, t, lr=1e-3).item()
+    assert l1 < l0
+
+
+def test_backward_refuses_batches_not_multiple_of_8(monkeypatch):
+    from mbsolve_gb300 import surrogate as S
+    E.install(monkeypatch)
+    sh = S.Shapes(S=64, W=8, Mo=8, L=2, F=8, Hq=16)
+    net = S.FNO(sh, seed=1, device="cpu")
+    net.forward(torch.zeros(4, sh.S, sh.F))
+    with pytest.raises(ValueError):
+        net.backward()
+
+
+def test_sweep_space_is_deterministic():
+    from mbsolve_gb300 import prescreen as P
+    a, b = P.SweepSpace(seed=0), P.SweepSpace(seed=0)
+    assert a.f0 == b.f0 and 3e12 <= a.f0 <= 8e12
+    pa, pb = a.sample(16, seed=5), b.sample(16, seed=5)
+    for k in P.PARAM_NAMES:
+        np.testing.assert_array_equal(pa[k], pb[k])
+        lo, hi = P.RANGES[k]
+        assert pa[k].min() >= lo and pa[k].max() <= hi
+    X = a.features(pa, device="cpu")
+    assert tuple(X.shape) == (16, a.samples, P.NUM_FEATURES)
+    assert float(X[..., 0].max()) <= 1.0 + 1e-6
+    assert float(X[..., 1:8].abs().max()) <= 1.0 + 1e-6
+    dev, sce = a.run(pa, 0)
+    assert sce.get_num_gridpoints() == a.n_x
