@@ -56,6 +56,8 @@ def parse():
                    help="skip the CPU-baseline sample")
     p.add_argument("--no-extras", action="store_true",
                    help="only the headline measurement")
+    p.add_argument("--no-surrogate", action="store_true",
+                   help="skip the surrogate (FNO) prescreen pipeline")
     p.add_argument("--tuning", default="",
                    help="C,NT,DEPTH to fix the launch shape (default: "
                         "autotuned)")
@@ -234,6 +236,79 @@ def cpu_sample(seed, target_s=12.0, threads=None):
             "oracle restating solver_cpu_fdtd<2, cvr_rodr>, OpenMP over "
             "points" % (total_cells, steps))
     return cu / dt, desc, threads, cu, dt
+
+
+def _timed_single_run(solver, dev, sce, n_t, warm=200, tail=200):
+    """Cell-updates/s of one run over n_t - warm - tail timed steps (CUDA
+    events on the run's stream, after autotuning and warm-up), and the
+    probe trace of all n_t steps."""
+    e = ensemble.ensemble(solver, [(dev, sce)])
+    nx = e.grid(0).num_gridpoints
+    e.advance(warm)
+    e.region_begin()
+    e.advance(n_t - warm - tail)
+    ms = e.region_end()
+    e.run()
+    probe = e.results(0)[0].as_array().ravel()
+    tun = e.info()
+    del e
+    return nx * (n_t - warm - tail) / (ms * 1e-3), probe, tun
+
+
+def config_extras():
+    """The 6-level (Rodrigues and Cayley) and 3-level Lambda (Cayley)
+    workloads at their full grid sizes over truncated runs, FP32 against
+    FP64; errors of FP32 vs FP64 on the probe traces."""
+    out = {}
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    n_t = 2000
+    for algo in ("cvr-rodr", "reg-cayley"):
+        r = {}
+        for prec in ("fp64", "fp32"):
+            mb.material.clear_library()
+            dev, sce = setups.random_nlvl(N=6, num_gridpoints=65536,
+                                          num_timesteps=n_t, seed=0)
+            r[prec] = _timed_single_run("gpu-fdtd-6lvl-%s-%s" % (algo, prec),
+                                        dev, sce, n_t)
+        out["6lvl_" + algo] = {
+            "workload": "6-level random medium (seed 0), 65,536 points, "
+                        "CW seed 1e5 V/m; %d of %d steps timed" % (n_t - 400, n_t),
+            "fp64": r["fp64"][0], "fp32": r["fp32"][0],
+            "unit": "cell-updates/s", "fp32_over_fp64": r["fp32"][0] / r["fp64"][0],
+            "fp32_vs_fp64_probe_rel_l2": rel(r["fp32"][1], r["fp64"][1]),
+            "fp32_tuning": r["fp32"][2]}
+    r = {}
+    for prec in ("fp64", "fp32"):
+        mb.material.clear_library()
+        dev, sce = setups.lambda_3lvl(num_gridpoints=1048576, num_timesteps=n_t)
+        r[prec] = _timed_single_run("gpu-fdtd-3lvl-reg-cayley-" + prec, dev, sce, n_t)
+    err = {}
+    n_e = 60000
+    for prec in ("fp64", "fp32"):
+        mb.material.clear_library()
+        dev, sce = setups.lambda_3lvl(num_gridpoints=65536, num_timesteps=n_e,
+                                      probe=2e-6)
+        s_ = solvergpu.solver_gpu_fdtd(dev, sce, "gpu-fdtd-3lvl-reg-cayley-" + prec)
+        s_.run()
+        err[prec] = s_.get_results()[0].as_array().ravel()
+    out["3lvl_lambda_cayley"] = {
+        "workload": "3-level Lambda, 1,048,576 points, two sech pulses 200 fs "
+                    "apart; %d of %d steps timed" % (n_t - 400, n_t),
+        "fp64": r["fp64"][0], "fp32": r["fp32"][0], "unit": "cell-updates/s",
+        "fp32_over_fp64": r["fp32"][0] / r["fp64"][0],
+        "fp32_tuning": r["fp32"][2],
+        "fp32_vs_fp64_probe_rel_l2": rel(err["fp32"], err["fp64"]),
+        "error_workload": "same medium and pulses, 65,536 points, %d steps "
+                          "(both pulses pass), probe 2 um from the input" % n_e}
+    return out
+
+
+def surrogate_extras():
+    """Surrogate pipeline: 20,000 solver runs -> FNO trained on the GPU ->
+    10,000-point sweep, every point judged by the solver."""
+    from mbsolve_gb300 import prescreen
+    rep, _ = prescreen.pipeline(n_train=20000, n_sweep=10000, epochs=20)
+    return rep
 
 
 def run_reference_arm(args, dist):
@@ -475,6 +550,9 @@ def run_ours(args, dist):
                         "D2H of the step's probe samples",
         }
         del e
+        extras["configs"] = config_extras()
+        if not args.no_surrogate:
+            extras["surrogate"] = surrogate_extras()
         line.update(extras)
     elif dist.rank == 0:
         line["e2e"] = None

@@ -18,7 +18,26 @@ void launch_step(const kparams<T>& p, unsigned grid, size_t smem, cudaStream_t s
     step_kernel<T, ALGO, LEV, C, NT><<<grid, NT, smem, s>>>(p);
 }
 
+// FP32 coherence-vector kernels for 4-6 levels with the density products
+// of uniform tiles on the tensor cores (128 threads, one point each).
+template<int LEV>
+void launch_step_tc(const kparams<float>& p, unsigned grid, size_t smem, cudaStream_t s)
+{
+    constexpr int D = LEV * LEV - 1;
+    const size_t need = ((cvr_pad<float, D>::len * sizeof(float) + 127) & ~(size_t) 127) + 128 +
+        tc::shape<D>::BYTES;
+    if (smem < need) smem = need;
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        step_kernel<float, 1, LEV, 1, tc::M, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) need);
+    (void) attr;
+    step_kernel<float, 1, LEV, 1, tc::M, true><<<grid, tc::M, smem, s>>>(p);
+}
+
 }  // namespace mbg
+
+#define MBG_REG_CVR_TC(LEV)                                                       \
+    static const bool MBG_CAT(mbg_reg_, __LINE__) = ::mbg::register_kernel<float>( \
+        ::mbg::ALGO_CVR, LEV, 1, ::mbg::tc::M, &::mbg::launch_step_tc<LEV>);
 
 #define MBG_CAT2(a, b) a##b
 #define MBG_CAT(a, b) MBG_CAT2(a, b)

@@ -9,6 +9,7 @@
 #include <type_traits>
 
 #include "kernels.cuh"
+#include "tc_density.cuh"
 
 namespace mbg {
 
@@ -31,8 +32,9 @@ struct tile_lists {
     rec_desc rec[TILE_MAX_REC];
 };
 
-template<typename T, int ALGO, int LEV, int C, int NT, bool UNIFORM>
-__device__ __forceinline__ void tile_steps(
+// Returns false when a tensor-core wait ran out (TC kernels only).
+template<typename T, int ALGO, int LEV, int C, int NT, bool UNIFORM, bool TC = false>
+__device__ __forceinline__ bool tile_steps(
     const kparams<T>& p,
     const tile_desc& td,
     const run_desc& rd,
@@ -52,11 +54,14 @@ __device__ __forceinline__ void tile_steps(
     T* sh_a,
     T* sh_al,
     T* sh_b,
-    T* sh_bl)
+    T* sh_bl,
+    tc::ctx* tcc = nullptr)
 {
     constexpr bool DF = sizeof(T) == 4;
     constexpr int D = density_len<ALGO, LEV>::value;
     constexpr int NW = NT / 32;
+    constexpr bool TCU = TC && UNIFORM;  // density products on the tensor cores
+    static_assert(!TC || (DF && ALGO == 1 && D >= 15 && C == 1 && NT == tc::M), "TC kernel shape");
     // 2-level coefficients live in registers on uniform tiles; for 4 and more
     // levels uniform tiles hold the padded copy of cvr_pad in shared memory
     constexpr bool REGCOEF = UNIFORM && ALGO == 1 && D == 3;
@@ -155,7 +160,23 @@ __device__ __forceinline__ void tile_steps(
             }
         }
         // ---- density matrix and polarisation current at every point
-        if constexpr (D > 0) {
+        if constexpr (TCU) {
+            // all threads take part in the CTA-wide products; threads
+            // without a point pass zeros and keep their zero state
+            if (qm_uniform) {
+                const bool act = M[0] >= 0;
+                const float e = act ? E[0] + El[0] : 0.0f;
+                float pn = 0.0f;
+                const cvr_coef_pad<T, D> cf{ (uint32_t) __cvta_generic_to_shared(sh_coef), sh_coef };
+                if (!tc::cvr_update_df_tc<D>(*tcc, R[0], Rl[0], e, pn, cf)) return false;
+                if (act) {
+                    P[0] = pn;
+                } else {
+#pragma unroll
+                    for (int v = 0; v < D; v++) R[0][v] = Rl[0][v] = T(0);
+                }
+            }
+        } else if constexpr (D > 0) {
 #pragma unroll
             for (int j = 0; j < C; j++) {
                 if (M[j] < 0) continue;
@@ -233,9 +254,12 @@ __device__ __forceinline__ void tile_steps(
             }
         }
     }
+    return true;
 }
 
-template<typename T, int ALGO, int LEV, int C, int NT>
+// One launch: every tile advances by nsub steps. TC: 4-6 levels in FP32
+// with the density products of uniform tiles on the tensor cores.
+template<typename T, int ALGO, int LEV, int C, int NT, bool TC = false>
 __global__ void __launch_bounds__(NT) step_kernel(const kparams<T> p)
 {
     constexpr bool DF = sizeof(T) == 4;
@@ -327,6 +351,25 @@ __global__ void __launch_bounds__(NT) step_kernel(const kparams<T> p)
         }
         if constexpr (!DF) El[j] = Hl[j] = T(0);
     }
+    // tensor memory and the completion barrier of the TC kernels
+    __shared__ __align__(8) uint64_t tc_mbar;
+    __shared__ uint32_t tc_tmem;
+    tc::ctx tcc{};
+    if constexpr (TC) {
+        if (threadIdx.x < 32) {
+            asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                             (uint32_t) __cvta_generic_to_shared(&tc_tmem)),
+                         "r"(tc::TMEM_COLS)
+                         : "memory");
+            asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        }
+        if (threadIdx.x == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t) __cvta_generic_to_shared(&tc_mbar))
+                         : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        tc::fence_before();
+    }
     const bool uniform = td.uniform_mat >= 0;
     if (uniform) {
         const T* src = p.mc + (uint64_t) td.uniform_mat * p.mstride;
@@ -342,12 +385,41 @@ __global__ void __launch_bounds__(NT) step_kernel(const kparams<T> p)
     }
     __syncthreads();
 
-    if (uniform)
-        tile_steps<T, ALGO, LEV, C, NT, true>(p, td, rd, l0, nsteps, step0, E, El, H, Hl, P, R, Rl, M,
-                                              sh_coef, tl, sh_a, sh_al, sh_b, sh_bl);
-    else
+    if constexpr (TC) {
+        tc::fence_after();
+        const uint32_t ops = ((uint32_t) __cvta_generic_to_shared(smem_raw) +
+                              (uint32_t) (cvr_pad<T, D>::len * sizeof(T)) + 127u) & ~127u;
+        using TS = tc::shape<D>;
+        tcc.a_hi = ops;
+        tcc.a_lo = ops + TS::A_BYTES;
+        tcc.b_hi = ops + 2u * TS::A_BYTES;
+        tcc.b_lo = tcc.b_hi + TS::B_BYTES;
+        tcc.b_dl = tcc.b_lo + TS::B_BYTES;
+        tcc.tmem = tc_tmem;
+        tcc.mbar = (uint32_t) __cvta_generic_to_shared(&tc_mbar);
+        tcc.phase = 0;
+        if (uniform) tc::stage_b<D>(tcc, reinterpret_cast<const float*>(sh_coef));
+    }
+
+    if (uniform) {
+        const bool ok = tile_steps<T, ALGO, LEV, C, NT, true, TC>(p, td, rd, l0, nsteps, step0, E, El, H, Hl, P,
+                                                                  R, Rl, M, sh_coef, tl, sh_a, sh_al, sh_b,
+                                                                  sh_bl, &tcc);
+        if (!ok && threadIdx.x == 0) atomicOr(p.status, STATUS_TC_WAIT);
+    } else {
         tile_steps<T, ALGO, LEV, C, NT, false>(p, td, rd, l0, nsteps, step0, E, El, H, Hl, P, R, Rl, M,
                                                sh_coef, tl, sh_a, sh_al, sh_b, sh_bl);
+    }
+    if constexpr (TC) {
+        tc::fence_before();
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            tc::fence_after();
+            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tcc.tmem),
+                         "r"(tc::TMEM_COLS)
+                         : "memory");
+        }
+    }
 
     // Cayley, FP32: renormalise the trace to that of the initial density
     // matrix, in FP64, once per launch (the exact propagators preserve it:

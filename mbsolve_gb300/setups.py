@@ -255,7 +255,7 @@ def random_nlvl(N=6, num_gridpoints=65536, num_timesteps=200000, seed=0,
 
 
 def lambda_3lvl(num_gridpoints=1048576, num_timesteps=500000,
-                length=None, separation=200e-15):
+                length=None, separation=200e-15, probe=None):
     """3-level Lambda medium: levels 0 and 2 coupled to the upper level 1
     by dipoles; two sech pulses 200 fs apart, the second at a 10 % higher
     carrier frequency; probe at the output facet."""
@@ -280,5 +280,5 @@ def lambda_3lvl(num_gridpoints=1048576, num_timesteps=500000,
                                  2e14, 15.0, BETA))
     sce.add_source(mb.sech_pulse("sech2", 0.0, mb.source.soft_source, a,
                                  2.2e14, 15.0 + separation * BETA, BETA))
-    sce.add_record(mb.record("e", 0.0, length))
+    sce.add_record(mb.record("e", 0.0, length if probe is None else probe))
     return dev, sce

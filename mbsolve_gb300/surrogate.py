@@ -302,3 +302,49 @@ class FNO:
         self.backward()
         self.adam(lr=lr, weight_decay=weight_decay)
         return loss
+
+
+def main(argv=None):
+    """Time training steps (forward, loss, backward, Adam) and inference on
+    random inputs: python -m mbsolve_gb300.surrogate [--batch 64]
+    [--steps 50] [--samples 1024] [--width 64] [--modes 32] [--layers 4]."""
+    import argparse
+    import json
+    import time
+    ap = argparse.ArgumentParser(description="surrogate step timing")
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--samples", type=int, default=1024)
+    ap.add_argument("--width", type=int, default=64)
+    ap.add_argument("--modes", type=int, default=32)
+    ap.add_argument("--layers", type=int, default=4)
+    ap.add_argument("--features", type=int, default=9)
+    a = ap.parse_args(argv)
+    sh = Shapes(S=a.samples, W=a.width, Mo=a.modes, L=a.layers, F=a.features)
+    net = FNO(sh, seed=0)
+    g = torch.Generator(device="cpu").manual_seed(0)
+    X = torch.randn(a.batch, sh.S, sh.F, generator=g).cuda()
+    t = torch.randn(a.batch, sh.S, generator=g).cuda()
+    for _ in range(3):
+        net.train_step(X, t)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        loss = net.train_step(X, t)
+    torch.cuda.synchronize()
+    dt_train = (time.perf_counter() - t0) / a.steps
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        net.forward(X)
+    torch.cuda.synchronize()
+    dt_fwd = (time.perf_counter() - t0) / a.steps
+    print(json.dumps({"shapes": vars(sh), "batch": a.batch,
+                      "train_step_ms": dt_train * 1e3,
+                      "forward_ms": dt_fwd * 1e3,
+                      "samples_per_s_train": a.batch / dt_train,
+                      "samples_per_s_forward": a.batch / dt_fwd,
+                      "loss": float(loss.item()), "status": K.status()}))
+
+
+if __name__ == "__main__":
+    main()
