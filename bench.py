@@ -242,6 +242,7 @@ def _timed_single_run(solver, dev, sce, n_t, warm=200, tail=200):
     """Cell-updates/s of one run over n_t - warm - tail timed steps (CUDA
     events on the run's stream, after autotuning and warm-up), and the
     probe trace of all n_t steps."""
+    from mbsolve_gb300 import ensemble
     e = ensemble.ensemble(solver, [(dev, sce)])
     nx = e.grid(0).num_gridpoints
     e.advance(warm)
@@ -259,6 +260,9 @@ def config_extras():
     """The 6-level (Rodrigues and Cayley) and 3-level Lambda (Cayley)
     workloads at their full grid sizes over truncated runs, FP32 against
     FP64; errors of FP32 vs FP64 on the probe traces."""
+    import numpy as np
+    from mbsolve_gb300 import lib as mb
+    from mbsolve_gb300 import setups, solvergpu
     out = {}
     rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
     n_t = 2000

@@ -315,8 +315,19 @@ int mbg_ensemble_stream_time(mbg_ensemble* e, int begin, double* milliseconds);
 /* Kernels this library launched on the ensemble's stream so far (time-step
  * kernels and the small clock/gather kernels around them). */
 int mbg_ensemble_launches(const mbg_ensemble* e, uint64_t* launches);
-/* Status flags raised on the device (bit 0: non-finite probe value). */
+/* Status flags raised on the device (bit 0: non-finite probe value;
+ * bit 3: a tensor-core completion wait ran out). */
 int mbg_ensemble_status(mbg_ensemble* e, uint32_t* flags);
+/* Checkpoint and resume (no reference counterpart; the reference has no
+ * checkpointing). The state is every field, density and record value plus
+ * the step index, in host memory: mbg_ensemble_state_size gives the bytes,
+ * mbg_ensemble_save_state writes them (after the queued work finishes),
+ * mbg_ensemble_load_state restores them into an ensemble created from the
+ * same descriptions (refused with MBG_ERR_INVALID_ARGUMENT otherwise);
+ * advancing it then continues exactly where the saved one stood. */
+int mbg_ensemble_state_size(const mbg_ensemble* e, uint64_t* bytes);
+int mbg_ensemble_save_state(mbg_ensemble* e, void* host, uint64_t bytes);
+int mbg_ensemble_load_state(mbg_ensemble* e, const void* host, uint64_t bytes);
 void mbg_ensemble_destroy(mbg_ensemble* e);
 
 /* ------------------------------------------------------------ inspection */

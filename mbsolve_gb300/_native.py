@@ -85,6 +85,9 @@ def load():
     L.mbg_material_layout.restype = C.c_size_t
     L.mbg_material_layout.argtypes = [C.c_char_p, C.c_uint32, C.c_char_p,
                                       C.c_size_t]
+    L.mbg_ensemble_state_size.argtypes = [C.c_void_p, P(C.c_uint64)]
+    L.mbg_ensemble_save_state.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64]
+    L.mbg_ensemble_load_state.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64]
     # include/mbsolve_fno.h
     vp, i32, i64, f32, f64 = C.c_void_p, C.c_int32, C.c_int64, C.c_float, C.c_double
     L.mbg_fno_gemm.argtypes = [P(T.mbg_gemm_desc), vp]

@@ -130,8 +130,8 @@ int mbg_solver_run(mbg_solver* s)
         // time index (sources, record rows) starting at 0
         s->eng->restart_clock();
         s->eng->advance(s->eng->steps_total());
-        uint32_t st = s->eng->status();
-        (void) st;
+        const uint32_t st = s->eng->status();
+        if (st & mbg::STATUS_TC_WAIT) throw std::runtime_error("CUDA: a tensor-core completion wait ran out");
     });
 }
 
@@ -325,6 +325,30 @@ int mbg_ensemble_launches(const mbg_ensemble* e, uint64_t* launches)
     return guarded([&] {
         if (!e || !launches) throw mbg::invalid_argument("null argument");
         *launches = e->eng->launches();
+    });
+}
+
+int mbg_ensemble_state_size(const mbg_ensemble* e, uint64_t* bytes)
+{
+    return guarded([&] {
+        if (!e || !bytes) throw mbg::invalid_argument("null argument");
+        *bytes = e->eng->state_bytes();
+    });
+}
+
+int mbg_ensemble_save_state(mbg_ensemble* e, void* host, uint64_t bytes)
+{
+    return guarded([&] {
+        if (!e) throw mbg::invalid_argument("null argument");
+        e->eng->save_state(host, bytes);
+    });
+}
+
+int mbg_ensemble_load_state(mbg_ensemble* e, const void* host, uint64_t bytes)
+{
+    return guarded([&] {
+        if (!e) throw mbg::invalid_argument("null argument");
+        e->eng->load_state(host, bytes);
     });
 }
 

@@ -594,6 +594,85 @@ public:
         MBG_CK(cudaGetLastError());
     }
 
+    // ------------------------------------------------------ checkpoints
+    struct state_header {
+        char magic[8];
+        uint32_t version, real_bytes, algo, levels;
+        uint64_t n_total, planes, scratch, runs, nt_max, steps_done;
+    };
+
+    uint64_t state_bytes() const override
+    {
+        const uint64_t words = n_total_ * (3 + (DF ? 2 : 0)) + n_total_ * (uint64_t) planes_ + scratch_.n;
+        return sizeof(state_header) + words * sizeof(T);
+    }
+
+    state_header header() const
+    {
+        state_header h{};
+        std::memcpy(h.magic, "MBGSTATE", 8);
+        h.version = 1;
+        h.real_bytes = sizeof(T);
+        h.algo = (uint32_t) kind_.algo;
+        h.levels = (uint32_t) kind_.N;
+        h.n_total = n_total_;
+        h.planes = (uint64_t) planes_;
+        h.scratch = scratch_.n;
+        h.runs = runs_.size();
+        h.nt_max = nt_max_;
+        h.steps_done = steps_done_;
+        return h;
+    }
+
+    template<typename F>
+    void state_arrays(F&& f)
+    {
+        f(E_[cur_].p, n_total_);
+        f(H_[cur_].p, n_total_);
+        f(P_[cur_].p, n_total_);
+        if (DF) {
+            f(El_[cur_].p, n_total_);
+            f(Hl_[cur_].p, n_total_);
+        }
+        if (planes_) f(D_[cur_].p, n_total_ * (uint64_t) planes_);
+        f(scratch_.p, (uint64_t) scratch_.n);
+    }
+
+    void save_state(void* host, uint64_t bytes) override
+    {
+        if (!host || bytes < state_bytes()) throw invalid_argument("state buffer too small");
+        const state_header h = header();
+        std::memcpy(host, &h, sizeof(h));
+        char* o = static_cast<char*>(host) + sizeof(h);
+        MBG_CK(cudaStreamSynchronize(stream_));
+        state_arrays([&](T* p, uint64_t n) {
+            MBG_CK(cudaMemcpy(o, p, n * sizeof(T), cudaMemcpyDeviceToHost));
+            o += n * sizeof(T);
+        });
+    }
+
+    void load_state(const void* host, uint64_t bytes) override
+    {
+        if (!host || bytes < sizeof(state_header)) throw invalid_argument("not a checkpoint");
+        state_header h;
+        std::memcpy(&h, host, sizeof(h));
+        const state_header m = header();
+        if (std::memcmp(h.magic, m.magic, 8) != 0 || h.version != m.version)
+            throw invalid_argument("not a checkpoint");
+        if (h.real_bytes != m.real_bytes || h.algo != m.algo || h.levels != m.levels || h.n_total != m.n_total ||
+            h.planes != m.planes || h.scratch != m.scratch || h.runs != m.runs || h.nt_max != m.nt_max)
+            throw invalid_argument("checkpoint does not match this ensemble");
+        if (bytes < state_bytes()) throw invalid_argument("checkpoint truncated");
+        if (h.steps_done > nt_max_) throw invalid_argument("checkpoint step out of range");
+        const char* i = static_cast<const char*>(host) + sizeof(h);
+        MBG_CK(cudaStreamSynchronize(stream_));
+        state_arrays([&](T* p, uint64_t n) {
+            MBG_CK(cudaMemcpy(p, i, n * sizeof(T), cudaMemcpyHostToDevice));
+            i += n * sizeof(T);
+        });
+        steps_done_ = h.steps_done;
+    }
+
     void copy_result(uint32_t run, uint32_t k, double* re, double* im) override
     {
         const run_setup& rs = runs_.at(run);

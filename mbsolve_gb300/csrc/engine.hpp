@@ -93,6 +93,12 @@ public:
     virtual uint64_t launches() const = 0;
     // begin: record a start event; else record a stop event, wait, return ms
     virtual double stream_time(bool begin) = 0;
+    // checkpoint of the full time-loop state (fields, density, records,
+    // step index) in host memory; load_state refuses a checkpoint of
+    // another ensemble shape
+    virtual uint64_t state_bytes() const = 0;
+    virtual void save_state(void* host, uint64_t bytes) = 0;
+    virtual void load_state(const void* host, uint64_t bytes) = 0;
 };
 
 std::unique_ptr<engine> make_engine(

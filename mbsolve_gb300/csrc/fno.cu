@@ -183,12 +183,11 @@ __device__ __forceinline__ float gelu_grad(float x)
 }
 
 // Gather 8 consecutive K elements (k0 .. k0+7, global K index) of row `row`
-// of operand A (is_a) or B into BF16 and store them as one 16-byte row of a
-// core matrix.
-__device__ __forceinline__ void load_chunk(
-    const gemm_params& p, bool is_a, int z, int row, int rows, int k0, uint32_t dst)
+// of operand A (is_a) or B, negated for a negated segment's A, zero outside
+// the operand.
+__device__ __forceinline__ void gather_chunk(
+    const gemm_params& p, bool is_a, int z, int row, int rows, int k0, float (&v)[8])
 {
-    float v[8];
 #pragma unroll
     for (int e = 0; e < 8; e++) v[e] = 0.0f;
     if (row < rows && k0 < p.ktotal) {
@@ -230,6 +229,11 @@ __device__ __forceinline__ void load_chunk(
             for (int e = 0; e < 8; e++) v[e] = -v[e];
         }
     }
+}
+
+// one 16-byte row of a core matrix, as BF16
+__device__ __forceinline__ void store_chunk(uint32_t dst, const float (&v)[8])
+{
     const uint32_t w0 = pack_bf16(v[0], v[1]), w1 = pack_bf16(v[2], v[3]);
     const uint32_t w2 = pack_bf16(v[4], v[5]), w3 = pack_bf16(v[6], v[7]);
     asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(dst), "r"(w0), "r"(w1), "r"(w2), "r"(w3)
@@ -242,39 +246,58 @@ __device__ __forceinline__ uint32_t chunk_off(int row, int kc)
     return (uint32_t) (((row >> 3) * (BK / 8) + kc) * 128 + (row & 7) * 16);
 }
 
-// Stage the A (BM x BK) and B (BN x BK) tiles of K block kb.
+constexpr int A_CHUNKS = BM * (BK / 8) / NTH;  // 8 per thread
+constexpr int B_CHUNKS = BN * (BK / 8) / NTH;  // 4 per thread
+
+// row and K chunk of chunk c: rows first when the operand's rows are
+// adjacent in memory (row stride 1), 16-byte K chunks first otherwise
+__device__ __forceinline__ void chunk_pos(int c, int R, bool rows_first, int& row, int& kc)
+{
+    if (rows_first) {
+        row = c % R;
+        kc = c / R;
+    } else {
+        row = (c >> 6) * 8 + (c & 7);
+        kc = (c >> 3) & 7;
+    }
+}
+
+// Stage the A (BM x BK) and B (BN x BK) tiles of K block kb: every global
+// load of the thread is issued before the first shared-memory store, so
+// that their latencies overlap.
 __device__ __forceinline__ void load_stage(
     const gemm_params& p, int z, int m0, int n0, int kb, uint32_t sa, uint32_t sb)
 {
     const int k0 = kb * BK;
-    // thread order: rows first when the block's operand rows are adjacent in
-    // memory (row stride 1), 16-byte K chunks first otherwise
     int s = 0;
     if (p.nseg > 1 && k0 >= p.kstart[1]) s = 1;
     if (p.nseg > 2 && k0 >= p.kstart[2]) s = 2;
     const bool a_rows = p.seg[s].a_sm == 1;
     const bool b_rows = p.seg[s].b_sn == 1;
-    for (int c = threadIdx.x; c < BM * (BK / 8); c += NTH) {
+    float va[A_CHUNKS][8], vb[B_CHUNKS][8];
+#pragma unroll
+    for (int i = 0; i < A_CHUNKS; i++) {
         int row, kc;
-        if (a_rows) {
-            row = c % BM;
-            kc = c / BM;
-        } else {
-            row = (c >> 6) * 8 + (c & 7);
-            kc = (c >> 3) & 7;
-        }
-        load_chunk(p, true, z, m0 + row, p.m, k0 + kc * 8, sa + chunk_off(row, kc));
+        chunk_pos(threadIdx.x + i * NTH, BM, a_rows, row, kc);
+        gather_chunk(p, true, z, m0 + row, p.m, k0 + kc * 8, va[i]);
     }
-    for (int c = threadIdx.x; c < BN * (BK / 8); c += NTH) {
+#pragma unroll
+    for (int i = 0; i < B_CHUNKS; i++) {
         int row, kc;
-        if (b_rows) {
-            row = c % BN;
-            kc = c / BN;
-        } else {
-            row = (c >> 6) * 8 + (c & 7);
-            kc = (c >> 3) & 7;
-        }
-        load_chunk(p, false, z, n0 + row, p.n, k0 + kc * 8, sb + chunk_off(row, kc));
+        chunk_pos(threadIdx.x + i * NTH, BN, b_rows, row, kc);
+        gather_chunk(p, false, z, n0 + row, p.n, k0 + kc * 8, vb[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < A_CHUNKS; i++) {
+        int row, kc;
+        chunk_pos(threadIdx.x + i * NTH, BM, a_rows, row, kc);
+        store_chunk(sa + chunk_off(row, kc), va[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < B_CHUNKS; i++) {
+        int row, kc;
+        chunk_pos(threadIdx.x + i * NTH, BN, b_rows, row, kc);
+        store_chunk(sb + chunk_off(row, kc), vb[i]);
     }
 }
 

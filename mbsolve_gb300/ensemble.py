@@ -130,6 +130,29 @@ class ensemble:
         _native.check(self._L.mbg_ensemble_status(self._h, C.byref(f)))
         return f.value
 
+    def save_state(self):
+        """Checkpoint: the full time-loop state as a numpy uint8 array."""
+        n = C.c_uint64()
+        _native.check(self._L.mbg_ensemble_state_size(self._h, C.byref(n)))
+        buf = np.empty(n.value, dtype=np.uint8)
+        _native.check(self._L.mbg_ensemble_save_state(
+            self._h, buf.ctypes.data_as(C.c_void_p), n.value))
+        return buf
+
+    def load_state(self, buf):
+        """Resume from save_state() of an ensemble of the same runs."""
+        buf = np.ascontiguousarray(buf, dtype=np.uint8)
+        _native.check(self._L.mbg_ensemble_load_state(
+            self._h, buf.ctypes.data_as(C.c_void_p), buf.size))
+
+    def save(self, path):
+        with open(path, "wb") as f:
+            f.write(self.save_state().tobytes())
+
+    def load(self, path):
+        with open(path, "rb") as f:
+            self.load_state(np.frombuffer(f.read(), dtype=np.uint8))
+
     def close(self):
         if getattr(self, "_h", None):
             self._L.mbg_ensemble_destroy(self._h)

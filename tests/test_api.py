@@ -16,7 +16,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _declared():
-    src = open(os.path.join(ROOT, "include", "mbsolve_gb300.h")).read()
+    src = open(os.path.join(ROOT, "include", "mbsolve_gb300.h")).read() + \
+        open(os.path.join(ROOT, "include", "mbsolve_fno.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     return sorted(set(re.findall(r"\b(mbg_[a-z_0-9]+)\s*\(", src)))
 
