@@ -24,7 +24,7 @@ template<int LEV>
 void launch_step_tc(const kparams<float>& p, unsigned grid, size_t smem, cudaStream_t s)
 {
     constexpr int D = LEV * LEV - 1;
-    const size_t need = ((cvr_pad<float, D>::len * sizeof(float) + 127) & ~(size_t) 127) + 128 +
+    const size_t need = ((tc::coef_small<D>::len * sizeof(float) + 127) & ~(size_t) 127) + 128 +
         tc::shape<D>::BYTES;
     if (smem < need) smem = need;
     static const cudaError_t attr = cudaFuncSetAttribute(

@@ -79,6 +79,7 @@ __device__ __forceinline__ float tf32_hi(float x)
 
 struct ctx {
     uint32_t a_hi, a_lo, b_hi, b_lo, b_dl;
+    float* rows;  // the A_hi region as plain rows of V floats (mixed tiles)
     uint32_t tmem;
     uint32_t mbar;
     uint32_t phase;
@@ -137,13 +138,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
 }
 
 // Stage the B operands (Bd split into TF32 high and low parts, and Bdl)
-// from the padded shared copy (cvr_pad). Rows n >= V and columns k >= V
-// are zero. Called by all threads; a barrier must follow.
+// from the material block in global memory (layout of make_cvr_layout: Bd
+// at FDTD_END, Bdl after it, both V x V row-major). Rows n >= V and
+// columns k >= V are zero. Called by all threads; a barrier must follow.
 template<int V>
-__device__ __forceinline__ void stage_b(const ctx& c, const float* pad)
+__device__ __forceinline__ void stage_b(const ctx& c, const float* mat)
 {
-    using Lp = cvr_pad<float, V>;
     using S = shape<V>;
+    const float* bd = mat + pre::FDTD_END;
+    const float* bdl = bd + V * V;
     for (int e = threadIdx.x; e < S::N * S::KC; e += M) {
         const int n = e / S::KC, kc = e % S::KC;
         float h[4], l[4], dl[4];
@@ -151,10 +154,10 @@ __device__ __forceinline__ void stage_b(const ctx& c, const float* pad)
         for (int q = 0; q < 4; q++) {
             const int k = kc * 4 + q;
             const bool in = n < V && k < V;
-            const float b = in ? pad[Lp::oBd + n * Lp::VP + k] : 0.0f;
+            const float b = in ? bd[n * V + k] : 0.0f;
             h[q] = tf32_hi(b);
             l[q] = b - h[q];
-            dl[q] = in ? pad[Lp::oBdl + n * Lp::VP + k] : 0.0f;
+            dl[q] = in ? bdl[n * V + k] : 0.0f;
         }
         const uint32_t o = chunk<V>(n, kc);
         st16(c.b_hi + o, h[0], h[1], h[2], h[3]);
@@ -222,9 +225,10 @@ __device__ __forceinline__ bool product(ctx& c)
     return __syncthreads_and(ok) != 0;
 }
 
-// Row threadIdx.x of D0 (cols 0..V-1) into d, of D1 into dl.
-template<int V>
-__device__ __forceinline__ void read_row(const ctx& c, float (&d)[V], float (&dl)[V])
+// Row threadIdx.x of D0 and D1, 16 columns at a time: f(i, D0[i], D1[i])
+// for i < V (i a compile-time constant).
+template<int V, class F>
+__device__ __forceinline__ void consume_row(const ctx& c, F&& f)
 {
     const uint32_t lane = (uint32_t) ((threadIdx.x >> 5) * 32) << 16;
     static_for<0, (V + 15) / 16>([&](auto BI) {
@@ -235,58 +239,112 @@ __device__ __forceinline__ void read_row(const ctx& c, float (&d)[V], float (&dl
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         static_for<0, 16>([&](auto QI) {
             constexpr int q = decltype(QI)::value;
-            if constexpr (b * 16 + q < V) {
-                d[b * 16 + q] = v[q];
-                dl[b * 16 + q] = w[q];
-            }
+            if constexpr (b * 16 + q < V) f(std::integral_constant<int, b * 16 + q>{}, v[q], w[q]);
         });
     });
 }
 
+// Per-material values the tensor-core update reads besides Bd (k, g,
+// theta dt, p0): the FDTD head of the material block followed by its k, g
+// and theta dt, staged in shared memory.
+template<int V>
+struct coef_small {
+    static constexpr int len = pre::FDTD_END + 2 * V + (V / 2 > 0 ? V / 2 : 1);
+    const float* base;
+    __device__ __forceinline__ float k(int i) const { return base[pre::FDTD_END + i]; }
+    __device__ __forceinline__ float g(int i) const { return base[pre::FDTD_END + V + i]; }
+    __device__ __forceinline__ float th(int q) const { return base[pre::FDTD_END + 2 * V + q]; }
+    __device__ __forceinline__ float p0() const { return base[5]; }
+    // index in the material block (layout of make_cvr_layout) of entry i
+    __device__ __forceinline__ static int source(int i)
+    {
+        return i < pre::FDTD_END ? i : pre::FDTD_END + 2 * V * V + (i - pre::FDTD_END);
+    }
+};
+
 // The FP32 coherence-vector update of cvr_update_df with the two matrix
-// products on the tensor cores. All threads of the CTA call it (threads
-// without a point pass zeros and ignore the result).
+// products on the tensor cores. The products read their own copy of the
+// vector (shared memory), so the registers are updated in place. All
+// threads of the CTA call it (threads without a point pass zeros and
+// discard the result).
 template<int V, class CF>
 __device__ __forceinline__ bool cvr_update_df_tc(
     ctx& c, float (&uh)[V], float (&ul)[V], float e, float& pout, const CF& cf)
 {
-    float wh[V], wl[V];
-    float d[V], dl[V];
     write_row<V>(c, uh);
     if (!product<V>(c)) return false;
-    read_row<V>(c, d, dl);
-    static_for<0, V>([&](auto I) {
+    consume_row<V>(c, [&](auto I, float d, float dl) {
         constexpr int i = decltype(I)::value;
-        wh[i] = uh[i];
-        wl[i] = ul[i];
-        df_acc(wh[i], wl[i], cf.k(i) + d[i], dl[i]);
+        df_acc(uh[i], ul[i], cf.k(i) + d, dl);
     });
     static_for<0, V / 2>([&](auto KI) {
         constexpr int k = decltype(KI)::value;
         float sn, s2;
         rot_coeffs<float>(cf.th(k) * e, sn, s2);
-        const float a = wh[2 * k], b = wh[2 * k + 1];
+        const float a = uh[2 * k], b = uh[2 * k + 1];
         const float da = -fmaf(s2, a, sn * b);
         const float db = fmaf(sn, a, -s2 * b);
-        df_acc(wh[2 * k], wl[2 * k], da, 0.0f);
-        df_acc(wh[2 * k + 1], wl[2 * k + 1], db, 0.0f);
+        df_acc(uh[2 * k], ul[2 * k], da, 0.0f);
+        df_acc(uh[2 * k + 1], ul[2 * k + 1], db, 0.0f);
     });
     fence_before();   // the reads of D above precede the next product's MMAs
-    write_row<V>(c, wh);
+    write_row<V>(c, uh);
     if (!product<V>(c)) return false;
-    read_row<V>(c, d, dl);
     float pp = cf.p0();
-    static_for<0, V>([&](auto I) {
+    consume_row<V>(c, [&](auto I, float d, float dl) {
         constexpr int i = decltype(I)::value;
-        uh[i] = wh[i];
-        ul[i] = wl[i];
-        df_acc(uh[i], ul[i], cf.k(i) + d[i], dl[i]);
+        df_acc(uh[i], ul[i], cf.k(i) + d, dl);
         df_renorm(uh[i], ul[i]);
         pp = fmaf(cf.g(i), uh[i], fmaf(cf.g(i), ul[i], pp));
     });
     pout = pp;
     fence_before();
     return true;
+}
+
+// The same update on the CUDA cores with the point's own coefficients
+// (mixed-material tiles of the tensor-core kernel): the vector goes to this
+// thread's row of shared memory so that the products can update the
+// registers in place (the kernel's register budget has room for one
+// vector of hi and lo words, not two).
+template<int V, class CF>
+__device__ __forceinline__ void cvr_update_df_row(
+    float* row, float (&uh)[V], float (&ul)[V], float e, float& pout, const CF& cf)
+{
+    auto half_step = [&](bool last, float& pp) {
+        static_for<0, V>([&](auto J) {
+            constexpr int j = decltype(J)::value;
+            row[j] = uh[j];
+        });
+        static_for<0, V>([&](auto I) {
+            constexpr int i = decltype(I)::value;
+            float s = cf.k(i), sl = 0.0f;
+            for (int j = 0; j < V; j++) {
+                const float x = row[j];
+                s = fmaf(cf.Bd(i, j), x, s);
+                sl = fmaf(cf.Bdl(i, j), x, sl);
+            }
+            df_acc(uh[i], ul[i], s, sl);
+            if (last) {
+                df_renorm(uh[i], ul[i]);
+                pp = fmaf(cf.g(i), uh[i], fmaf(cf.g(i), ul[i], pp));
+            }
+        });
+    };
+    float pp = cf.p0();
+    half_step(false, pp);
+    static_for<0, V / 2>([&](auto KI) {
+        constexpr int k = decltype(KI)::value;
+        float sn, s2;
+        rot_coeffs<float>(cf.th(k) * e, sn, s2);
+        const float a = uh[2 * k], b = uh[2 * k + 1];
+        const float da = -fmaf(s2, a, sn * b);
+        const float db = fmaf(sn, a, -s2 * b);
+        df_acc(uh[2 * k], ul[2 * k], da, 0.0f);
+        df_acc(uh[2 * k + 1], ul[2 * k + 1], db, 0.0f);
+    });
+    half_step(true, pp);
+    pout = pp;
 }
 
 }  // namespace tc

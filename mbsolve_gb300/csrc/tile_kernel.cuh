@@ -167,7 +167,7 @@ __device__ __forceinline__ bool tile_steps(
                 const bool act = M[0] >= 0;
                 const float e = act ? E[0] + El[0] : 0.0f;
                 float pn = 0.0f;
-                const cvr_coef_pad<T, D> cf{ (uint32_t) __cvta_generic_to_shared(sh_coef), sh_coef };
+                const tc::coef_small<D> cf{ sh_coef };
                 if (!tc::cvr_update_df_tc<D>(*tcc, R[0], Rl[0], e, pn, cf)) return false;
                 if (act) {
                     P[0] = pn;
@@ -189,6 +189,11 @@ __device__ __forceinline__ bool tile_steps(
                             cvr_update_df<D>(R[j], Rl[j], e, P[j], creg);
                         else
                             cvr_update<T, D>(R[j], e, P[j], creg);
+                    } else if constexpr (TC) {
+                        // mixed tile of the tensor-core kernel: in place
+                        // through this thread's row of the idle A operand
+                        cvr_coef<T, D> cf{ cb };
+                        tc::cvr_update_df_row<D>(tcc->rows + threadIdx.x * D, R[j], Rl[j], e, P[j], cf);
                     } else if constexpr (PADC) {
                         const cvr_coef_pad<T, D> cf{ (uint32_t) __cvta_generic_to_shared(sh_coef), sh_coef };
                         if constexpr (DF)
@@ -260,7 +265,7 @@ __device__ __forceinline__ bool tile_steps(
 // One launch: every tile advances by nsub steps. TC: 4-6 levels in FP32
 // with the density products of uniform tiles on the tensor cores.
 template<typename T, int ALGO, int LEV, int C, int NT, bool TC = false>
-__global__ void __launch_bounds__(NT) step_kernel(const kparams<T> p)
+__global__ void __launch_bounds__(NT, TC ? 3 : 1) step_kernel(const kparams<T> p)
 {
     constexpr bool DF = sizeof(T) == 4;
     constexpr int D = density_len<ALGO, LEV>::value;
@@ -373,7 +378,10 @@ __global__ void __launch_bounds__(NT) step_kernel(const kparams<T> p)
     const bool uniform = td.uniform_mat >= 0;
     if (uniform) {
         const T* src = p.mc + (uint64_t) td.uniform_mat * p.mstride;
-        if constexpr (ALGO == 1 && D >= 15) {
+        if constexpr (TC) {
+            using Ls = tc::coef_small<D>;
+            for (int i = threadIdx.x; i < Ls::len; i += NT) sh_coef[i] = src[Ls::source(i)];
+        } else if constexpr (ALGO == 1 && D >= 15) {
             using Lp = cvr_pad<T, D>;
             for (int i = threadIdx.x; i < Lp::len; i += NT) {
                 const int q = Lp::source(i);
@@ -387,8 +395,9 @@ __global__ void __launch_bounds__(NT) step_kernel(const kparams<T> p)
 
     if constexpr (TC) {
         tc::fence_after();
-        const uint32_t ops = ((uint32_t) __cvta_generic_to_shared(smem_raw) +
-                              (uint32_t) (cvr_pad<T, D>::len * sizeof(T)) + 127u) & ~127u;
+        const uint32_t sbase = (uint32_t) __cvta_generic_to_shared(smem_raw);
+        const uint32_t ops = (sbase + (uint32_t) (tc::coef_small<D>::len * sizeof(T)) + 127u) & ~127u;
+        tcc.rows = reinterpret_cast<float*>(smem_raw + (ops - sbase));
         using TS = tc::shape<D>;
         tcc.a_hi = ops;
         tcc.a_lo = ops + TS::A_BYTES;
@@ -398,7 +407,7 @@ __global__ void __launch_bounds__(NT) step_kernel(const kparams<T> p)
         tcc.tmem = tc_tmem;
         tcc.mbar = (uint32_t) __cvta_generic_to_shared(&tc_mbar);
         tcc.phase = 0;
-        if (uniform) tc::stage_b<D>(tcc, reinterpret_cast<const float*>(sh_coef));
+        if (uniform) tc::stage_b<D>(tcc, p.mc + (uint64_t) td.uniform_mat * p.mstride);
     }
 
     if (uniform) {
