@@ -265,7 +265,7 @@ __device__ __forceinline__ bool tile_steps(
 // One launch: every tile advances by nsub steps. TC: 4-6 levels in FP32
 // with the density products of uniform tiles on the tensor cores.
 template<typename T, int ALGO, int LEV, int C, int NT, bool TC = false>
-__global__ void __launch_bounds__(NT, TC ? 3 : 1) step_kernel(const kparams<T> p)
+__global__ void __launch_bounds__(NT, TC ? (LEV <= 4 ? 4 : 3) : 1) step_kernel(const kparams<T> p)
 {
     constexpr bool DF = sizeof(T) == 4;
     constexpr int D = density_len<ALGO, LEV>::value;

@@ -158,8 +158,13 @@ class FNO:
 
     @staticmethod
     def _split(rows):
-        """K splits of a weight-gradient product over `rows` rows."""
-        return max(1, min(152, rows // 512))
+        """K splits of a weight-gradient product over `rows` rows (two
+        64-row K blocks per CTA)."""
+        return max(1, min(1024, rows // 128))
+
+    # the truncated DFT and its gradient contract over the S samples: split
+    # K 8 ways (atomic FP32 accumulation) so that B x 8 CTAs share the work
+    DFT_SPLIT = 8
 
     # ------------------------------------------------------------ forward
     def forward(self, X):
@@ -182,8 +187,10 @@ class FNO:
         for l in range(L):
             v, vh = b["v"][l], b["Vh"][l]
             # truncated DFT: Vh[b, c, m'] = sum_s F[m', s] v[b, s, c]
+            vh.zero_()
             K.gemm(W, 2 * Mo, [Seg(v, 0, 1, W, S * W, self.F, 0, S, 1, 0, S)],
-                   vh, 0, 2 * Mo, 1, W * 2 * Mo, batch=B)
+                   vh, 0, 2 * Mo, 1, W * 2 * Mo, batch=B,
+                   mode=T.MBG_GEMM_ATOMIC, split_k=self.DFT_SPLIT)
             # mode mixing, per mode m: Y[b, m, :] = blk[m] [Re; Im]
             blk = self.blk[l]
             K.gemm(B, 2 * W,
@@ -244,8 +251,10 @@ class FNO:
                    g["W%d" % l], 0, W, 1, mode=ATOM, split_k=self._split(R))
             K.colsum(dpre, R, W, W, g["bw%d" % l])
             # dY[b, m', o] = sum_s G[s, m'] dpre[b, s, o]
+            b["dY"].zero_()
             K.gemm(2 * Mo, W, [Seg(self.G, 0, 1, 2 * Mo, 0, dpre, 0, 1, W, S * W, S)],
-                   b["dY"], 0, W, 1, 2 * Mo * W, batch=B)
+                   b["dY"], 0, W, 1, 2 * Mo * W, batch=B,
+                   mode=T.MBG_GEMM_ATOMIC, split_k=self.DFT_SPLIT)
             dY = b["dY"]
             a_re = dict(a_sm=1, a_sk=2 * Mo * W, a_sz=W)
             b_v = dict(b_sn=2 * Mo, b_sk=W * 2 * Mo, b_sz=1)
