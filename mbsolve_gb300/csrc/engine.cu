@@ -3,6 +3,7 @@
 // precompute on the GPU, the tile plan, launch loop, CUDA graphs and the
 // autotuner.
 #include <algorithm>
+#include <cctype>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -506,6 +507,32 @@ static const int MAX_DEPTH = 256;
 
 static std::mutex g_tune_mutex;
 static std::map<std::string, tuning> g_tune_cache;
+static bool g_tune_file_read = false;
+
+// Autotuner results persist across processes in the file named by the
+// environment variable MBG_TUNE_CACHE, when it is set: one line
+// "key C NT depth graph" per tuned problem (keys contain the GPU's name).
+// Called with g_tune_mutex held.
+static void tune_file_read()
+{
+    if (g_tune_file_read) return;
+    g_tune_file_read = true;
+    const char* path = std::getenv("MBG_TUNE_CACHE");
+    if (!path || !path[0]) return;
+    std::ifstream f(path);
+    std::string key;
+    tuning t;
+    while (f >> key >> t.C >> t.NT >> t.depth >> t.graph)
+        if (t.C > 0 && t.NT > 0 && t.depth > 0) g_tune_cache[key] = t;
+}
+
+static void tune_file_append(const std::string& key, const tuning& t)
+{
+    const char* path = std::getenv("MBG_TUNE_CACHE");
+    if (!path || !path[0]) return;
+    std::ofstream f(path, std::ios::app);
+    if (f) f << key << " " << t.C << " " << t.NT << " " << t.depth << " " << t.graph << "\n";
+}
 
 template<typename T>
 class engine_t : public engine {
@@ -1169,6 +1196,12 @@ private:
     std::string tune_key() const
     {
         std::ostringstream s;
+        int dev = 0;
+        cudaDeviceProp prop;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaGetDeviceProperties(&prop, dev) == cudaSuccess) {
+            for (const char* c = prop.name; *c; c++) s << (std::isalnum((unsigned char) *c) ? *c : '_');
+            s << "_" << prop.multiProcessorCount << ":";
+        }
         s << kind_.algo << ":" << kind_.N << ":" << (kind_.fp64 ? 64 : 32) << ":"
           << (cells_ >> 16) << ":" << runs_.size() << ":" << std::min<uint64_t>(nt_max_, 256);
         return s.str();
@@ -1263,6 +1296,7 @@ private:
             bool cached = false;
             {
                 std::lock_guard<std::mutex> lk(g_tune_mutex);
+                tune_file_read();
                 auto it = g_tune_cache.find(key);
                 if (it != g_tune_cache.end()) {
                     t = it->second;
@@ -1299,6 +1333,7 @@ private:
                 t = best;
                 std::lock_guard<std::mutex> lk(g_tune_mutex);
                 g_tune_cache[key] = t;
+                tune_file_append(key, t);
             }
         }
         if (t.graph % 2) t.graph += 1;
