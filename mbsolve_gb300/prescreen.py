@@ -297,7 +297,7 @@ def delayed_input(space, X):
 
 def pipeline(n_train=20000, n_sweep=10000, n_judge=None, shapes=None,
              epochs=30, batch=64, lr=2e-3, seed=0, absorb=None,
-             solver="gpu-fdtd-6lvl-reg-cayley-fp32", log=None):
+             solver="gpu-fdtd-6lvl-cvr-rodr-fp32", log=None):
     """Generate training runs with the solver, train the surrogate on the
     GPU, sweep n_sweep new points with it and judge it with the solver on
     n_judge of them (all by default). The prescreen question is "which
