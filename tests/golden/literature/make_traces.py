@@ -1,10 +1,10 @@
-"""Builds tests/golden/literature.npz from the reference's literature
+"""Builds tests/golden/literature/traces.npz from the reference's literature
 traces (tools/reference-data/*.csv of the mbsolve tree, digitised from the
 papers its presets reproduce): x in um vs population inversion
 (Ziolkowski 1995, fig. 2, compared at record row 75 = 187.5 fs), t in fs vs
 rho11 (Song 2005, fig. 3a), t in ps vs rho55 and rho66 (Marskar 2011).
 
-    python tests/golden/make_literature.py [path/to/mbsolve]
+    python tests/golden/literature/make_traces.py [path/to/mbsolve]
 """
 import os
 import sys
@@ -23,7 +23,7 @@ def main():
                       ("marskar2011_d55", "marskar2011-rho55.csv"),
                       ("marskar2011_d66", "marskar2011-rho66.csv")]:
         out[key] = np.loadtxt(os.path.join(d, name), delimiter=",")
-    np.savez_compressed(os.path.join(HERE, "literature.npz"), **out)
+    np.savez_compressed(os.path.join(HERE, "traces.npz"), **out)
 
 
 if __name__ == "__main__":

@@ -1,6 +1,6 @@
 """Known-answer tests against the literature traces the reference ships
 (tools/reference-data, digitised from the papers; fixture built by
-tests/golden/make_literature.py). Plot-level tolerances: the traces are
+tests/golden/literature/make_traces.py). Plot-level tolerances: the traces are
 digitised curves. The FP64 oracle (CPU) and the GPU solvers (FP64 and
 FP32) must both reproduce them:
 
@@ -25,7 +25,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def _fixture():
-    return np.load(os.path.join(HERE, "golden", "literature.npz"))
+    return np.load(os.path.join(HERE, "golden", "literature", "traces.npz"))
 
 
 def _err(t, y, ref, tscale, shifts=(0.0,)):
