@@ -650,14 +650,17 @@ __device__ __forceinline__ void cayley_update(T (&rho)[N * N], T e, T& pout, con
             A[i][j].im = K[i][j].re;
             Y[i][j] = K[i][j];
         }
-    // solve A Y = K by LU without pivoting (A + A^H = 2I > 0)
+    // solve A Y = K by LU without pivoting (A + A^H = 2I > 0); the inverse
+    // of each pivot (one real division) serves elimination and
+    // back-substitution (a pivot is final once its step begins)
+    cx pinv[N];
 #pragma unroll
     for (int k = 0; k < N; k++) {
-        // inverse of the pivot
-        T den = A[k][k].re * A[k][k].re + A[k][k].im * A[k][k].im;
+        const T rden = T(1) / (A[k][k].re * A[k][k].re + A[k][k].im * A[k][k].im);
         cx inv;
-        inv.re = A[k][k].re / den;
-        inv.im = -A[k][k].im / den;
+        inv.re = A[k][k].re * rden;
+        inv.im = -A[k][k].im * rden;
+        pinv[k] = inv;
 #pragma unroll
         for (int i = k + 1; i < N; i++) {
             cx f;
@@ -677,10 +680,7 @@ __device__ __forceinline__ void cayley_update(T (&rho)[N * N], T e, T& pout, con
     }
 #pragma unroll
     for (int k = N - 1; k >= 0; k--) {
-        T den = A[k][k].re * A[k][k].re + A[k][k].im * A[k][k].im;
-        cx inv;
-        inv.re = A[k][k].re / den;
-        inv.im = -A[k][k].im / den;
+        const cx inv = pinv[k];
 #pragma unroll
         for (int j = 0; j < N; j++) {
             cx s = Y[k][j];
