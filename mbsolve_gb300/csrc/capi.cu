@@ -447,7 +447,7 @@ size_t mbg_material_layout(const char* algo, uint32_t N, char* buf, size_t len)
         s << "a=" << L.a << "\nb=" << L.b << "\ncH=" << L.cH << "\ngamma=" << L.gam << "\nhas_qm=" << L.has_qm
           << "\nkH0=" << L.kH0 << "\nkMu=" << L.kMu << "\nW0=" << L.W0 << "\nMn=" << L.Mn << "\ndD1=" << L.dD1
           << "\nd1=" << L.d1 << "\ndD2=" << L.dD2 << "\nd2=" << L.d2 << "\nrho0=" << L.rho0
-          << "\nstride=" << L.stride;
+          << "\ngP=" << L.gP << "\nstride=" << L.stride;
     }
     std::string t = s.str();
     if (buf && len) {

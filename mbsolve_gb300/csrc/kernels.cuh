@@ -779,63 +779,11 @@ __device__ __forceinline__ void cayley_update(T (&rho)[N * N], T e, T& pout, con
             rho[N + 2 * q] = A[j][k].re;
             rho[N + 2 * q + 1] = A[j][k].im;
         }
-    // P = Re tr(rhs Mn), rhs = -i [W0, rho] + D'(rho)
-    cx W[N][N], Mn[N][N];
-#pragma unroll
-    for (int i = 0; i < N; i++) {
-        W[i][i].re = cf[L.W0 + i];
-        W[i][i].im = T(0);
-        Mn[i][i].re = cf[L.Mn + i];
-        Mn[i][i].im = T(0);
-    }
-#pragma unroll
-    for (int k = 1; k < N; k++)
-#pragma unroll
-        for (int j = 0; j < k; j++) {
-            const int q = k * (k - 1) / 2 + j;
-            W[j][k].re = cf[L.W0 + N + 2 * q];
-            W[j][k].im = cf[L.W0 + N + 2 * q + 1];
-            W[k][j].re = W[j][k].re;
-            W[k][j].im = -W[j][k].im;
-            Mn[j][k].re = cf[L.Mn + N + 2 * q];
-            Mn[j][k].im = cf[L.Mn + N + 2 * q + 1];
-            Mn[k][j].re = Mn[j][k].re;
-            Mn[k][j].im = -Mn[j][k].im;
-        }
+    // P = Re tr((-i [W0, rho] + D'(rho)) Mn), linear in the packed density
+    // matrix: P = gP . rho (weights from the FP64 precompute)
     T acc = T(0);
 #pragma unroll
-    for (int j = 0; j < N; j++)
-#pragma unroll
-        for (int k = 0; k < N; k++) {
-            // comm_jk = sum_l W_jl rho_lk - rho_jl W_lk
-            cx cm;
-            cm.re = T(0);
-            cm.im = T(0);
-#pragma unroll
-            for (int l = 0; l < N; l++) {
-                cm.re += W[j][l].re * A[l][k].re - W[j][l].im * A[l][k].im -
-                    (A[j][l].re * W[l][k].re - A[j][l].im * W[l][k].im);
-                cm.im += W[j][l].re * A[l][k].im + W[j][l].im * A[l][k].re -
-                    (A[j][l].re * W[l][k].im + A[j][l].im * W[l][k].re);
-            }
-            // rhs_jk = -i comm_jk + D'
-            cx r;
-            r.re = cm.im;
-            r.im = -cm.re;
-            if (j == k) {
-                T s = T(0);
-#pragma unroll
-                for (int l = 0; l < N; l++) s += cf[L.d1 + j * N + l] * A[l][l].re;
-                r.re += s;
-            } else {
-                const int q = (j < k) ? k * (k - 1) / 2 + j : j * (j - 1) / 2 + k;
-                const T d2 = cf[L.d2 + q];
-                r.re += d2 * A[j][k].re;
-                r.im += d2 * A[j][k].im;
-            }
-            // Re(rhs_jk Mn_kj)
-            acc += r.re * Mn[k][j].re - r.im * Mn[k][j].im;
-        }
+    for (int i = 0; i < N * N; i++) acc = fma(cf[L.gP + i], rho[i], acc);
     pout = acc;
 }
 

@@ -156,7 +156,7 @@ MBG_HD cvr_layout make_cvr_layout(int N)
 struct cay_layout {
     int N, P;
     int a, b, cH, gam, has_qm;
-    int kH0, kMu, W0, Mn, dD1, d1, dD2, d2, rho0, stride;
+    int kH0, kMu, W0, Mn, dD1, d1, dD2, d2, rho0, gP, stride;
 };
 
 MBG_HD cay_layout make_cay_layout(int N)
@@ -187,6 +187,8 @@ MBG_HD cay_layout make_cay_layout(int N)
     L.d2 = o;
     o += (L.P > 0 ? L.P : 1);
     L.rho0 = o;
+    o += N * N;
+    L.gP = o;  // P = gP . (packed density matrix)
     o += N * N;
     L.stride = (o + 3) & ~3;
     return L;
@@ -856,6 +858,66 @@ MBG_HD void pack_hermitian(const double* re, const double* im, int N, double s, 
         }
 }
 
+// Entry (j, k) of a Hermitian matrix stored packed (diagonal, then the upper
+// triangle column-major as (re, im) pairs).
+MBG_HD void herm_at(const double* p, int N, int j, int k, double& re, double& im)
+{
+    if (j == k) {
+        re = p[j];
+        im = 0.0;
+    } else if (j < k) {
+        const int q = upper_index(j, k);
+        re = p[N + 2 * q];
+        im = p[N + 2 * q + 1];
+    } else {
+        const int q = upper_index(k, j);
+        re = p[N + 2 * q];
+        im = -p[N + 2 * q + 1];
+    }
+}
+
+// The polarisation current of the Cayley update (reg_cayley.hpp:258-267),
+// P = Re tr((-i [W0, rho] + D'(rho)) Mn), is real-linear in the packed
+// density matrix r: P = gP . r. With C = Mn W0 - W0 Mn (anti-Hermitian),
+// Re tr(-i [W0, rho] Mn) = Im tr(rho C), and for r's coordinates
+//   diagonal l:        Im C_ll + sum_j d1[j][l] Mn_jj
+//   Re rho_jk (j < k): 2 Im C_jk + 2 gamma_jk Re Mn_jk
+//   Im rho_jk (j < k): -2 Re C_jk + 2 gamma_jk Im Mn_jk
+// (gamma_jk the dephasing rate of the pair, D'(rho)_jk = gamma_jk rho_jk).
+// Evaluated per material in FP64; the kernels then need N^2 FMAs per point.
+MBG_HD void cay_polarisation_weights(const cay_layout& L, double* out)
+{
+    const int N = L.N;
+    const double* W = out + L.W0;
+    const double* Mn = out + L.Mn;
+    for (int j = 0; j < N; j++)
+        for (int k = j; k < N; k++) {
+            // C_jk = sum_l Mn_jl W_lk - W_jl Mn_lk
+            double cr = 0.0, ci = 0.0;
+            for (int l = 0; l < N; l++) {
+                double mr, mi, wr, wi;
+                herm_at(Mn, N, j, l, mr, mi);
+                herm_at(W, N, l, k, wr, wi);
+                cr += mr * wr - mi * wi;
+                ci += mr * wi + mi * wr;
+                herm_at(W, N, j, l, wr, wi);
+                herm_at(Mn, N, l, k, mr, mi);
+                cr -= wr * mr - wi * mi;
+                ci -= wr * mi + wi * mr;
+            }
+            if (j == k) {
+                double s = ci;
+                for (int i = 0; i < N; i++) s += out[L.d1 + i * N + j] * Mn[i];
+                out[L.gP + j] = s;
+            } else {
+                const int q = upper_index(j, k);
+                const double g2 = out[L.d2 + q];
+                out[L.gP + N + 2 * q] = 2.0 * ci + 2.0 * g2 * Mn[N + 2 * q];
+                out[L.gP + N + 2 * q + 1] = -2.0 * cr + 2.0 * g2 * Mn[N + 2 * q + 1];
+            }
+        }
+}
+
 // Cayley constants of one material (cay_layout of `Nsolver` levels).
 // Returns 0, 1 on a level-count mismatch, 3 for a relaxation superoperator
 // that is not of Lindblad form (reg_cayley.hpp:146-155).
@@ -897,6 +959,7 @@ MBG_HD int cay_precompute(const mat_in& m, int Nsolver, double* ws, double* out)
         out[L.rho0 + N + 2 * p] = m.rho_off_re[p];
         out[L.rho0 + N + 2 * p + 1] = m.rho_off_im[p];
     }
+    cay_polarisation_weights(L, out);
     return 0;
 }
 

@@ -102,3 +102,46 @@ def test_level_mismatch_is_rejected(native):
                                        None, 0, C.byref(n))
     assert rc == T.MBG_ERR_INVALID_ARGUMENT
     assert b"Unsupported superoperator" in native.mbg_last_error()
+
+
+@pytest.mark.parametrize("N", [2, 3, 5])
+def test_cayley_polarisation_weights(native, N):
+    """P = Re tr((-i [W0, rho] + D'(rho)) Mn) (reg_cayley.hpp:258-267) is
+    linear in the packed density matrix; the precomputed weights gP equal
+    the formula evaluated on each packed basis element, and give P of a
+    random density matrix."""
+    from mbsolve_gb300 import _native
+    dev, sce = setups.random_nlvl(N=N, num_gridpoints=16, num_timesteps=10,
+                                  seed=11)
+    b = mb.to_pod(dev, sce)
+    mat = b.device.materials[0]
+    L = _native.material_layout("reg-cayley", N)
+    c = _constants(native, "reg-cayley", mat, 2.5e-17)
+    pairs = [(j, k) for k in range(N) for j in range(k)]
+
+    def full(p):
+        m = np.diag(p[:N]).astype(complex)
+        for q, (j, k) in enumerate(pairs):
+            m[j, k] = p[N + 2 * q] + 1j * p[N + 2 * q + 1]
+            m[k, j] = np.conj(m[j, k])
+        return m
+
+    W = full(c[L["W0"]:L["W0"] + N * N])
+    Mn = full(c[L["Mn"]:L["Mn"] + N * N])
+    d1 = c[L["d1"]:L["d1"] + N * N].reshape(N, N)
+    d2 = c[L["d2"]:L["d2"] + len(pairs)]
+
+    def P(r):
+        rho = full(r)
+        rhs = -1j * (W @ rho - rho @ W)
+        rhs += np.diag(d1 @ np.real(np.diag(rho)))
+        for q, (j, k) in enumerate(pairs):
+            rhs[j, k] += d2[q] * rho[j, k]
+            rhs[k, j] += d2[q] * rho[k, j]
+        return np.real(np.trace(rhs @ Mn))
+
+    g = c[L["gP"]:L["gP"] + N * N]
+    want = np.array([P(np.eye(N * N)[i]) for i in range(N * N)])
+    np.testing.assert_allclose(g, want, rtol=1e-12, atol=1e-12 * np.abs(want).max())
+    r = np.random.default_rng(1).normal(size=N * N)
+    assert g @ r == pytest.approx(P(r), rel=1e-12)
