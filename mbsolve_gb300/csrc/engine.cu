@@ -1248,7 +1248,7 @@ private:
         return t;
     }
 
-    double time_candidate(const tuning& t)
+    double time_candidate(const tuning& t, int reps = 3)
     {
         tune_ = t;
         fn_ = find_kernel(t.C, t.NT);
@@ -1265,7 +1265,6 @@ private:
         MBG_CK(cudaEventCreate(&a));
         MBG_CK(cudaEventCreate(&b));
         MBG_CK(cudaEventRecord(a, stream_));
-        const int reps = 3;
         for (int i = 0; i < reps; i++) once();
         MBG_CK(cudaEventRecord(b, stream_));
         MBG_CK(cudaEventSynchronize(b));
@@ -1276,6 +1275,27 @@ private:
         MBG_CK(cudaGetLastError());
         const double steps = std::min<double>(t.depth, (double) nt_max_);
         return (double) cells_ * steps * reps / (ms * 1e-3);
+    }
+
+    // Close contenders (within `margin` of the best first timing) are timed
+    // again, round-robin over several trials so that clock or thermal drift
+    // affects them alike, and the best of each one's trials decides: a
+    // single short timing cannot separate shapes a few per cent apart.
+    tuning runoff(const std::vector<std::pair<tuning, double> >& first, double margin)
+    {
+        double top = 0;
+        for (const auto& c : first) top = std::max(top, c.second);
+        std::vector<tuning> cands;
+        for (const auto& c : first)
+            if (c.second >= top * (1.0 - margin)) cands.push_back(c.first);
+        std::vector<double> best(cands.size(), 0.0);
+        if (cands.size() > 1)
+            for (int trial = 0; trial < 3; trial++)
+                for (size_t i = 0; i < cands.size(); i++) best[i] = std::max(best[i], time_candidate(cands[i], 4));
+        size_t bi = 0;
+        for (size_t i = 1; i < cands.size(); i++)
+            if (best[i] > best[bi]) bi = i;
+        return cands[bi];
     }
 
     void choose_tuning(const mbg_tuning* user)
@@ -1305,31 +1325,26 @@ private:
             }
             if (!cached) {
                 // stage 1: launch shape at the default depth; stage 2: depth
-                tuning best = t;
-                double best_rate = -1;
+                // (each stage ends with a run-off of its close contenders)
+                std::vector<std::pair<tuning, double> > shapes;
                 for (const auto& e : kernel_registry<T>()) {
                     if (e.algo != kind_.algo || e.lev != kind_.N) continue;
                     tuning c = t;
                     c.C = e.C;
                     c.NT = e.NT;
                     if (align_halo(c.depth) * 4 > c.C * c.NT) continue;
-                    double r = time_candidate(c);
-                    if (r > best_rate) {
-                        best_rate = r;
-                        best = c;
-                    }
+                    shapes.push_back({ c, time_candidate(c) });
                 }
+                tuning best = shapes.empty() ? t : runoff(shapes, 0.10);
+                std::vector<std::pair<tuning, double> > depths;
                 for (int d : { 1, 2, 4, 8, 16, 32, 64 }) {
                     tuning c = best;
                     c.depth = d;
                     if (align_halo(d) * 4 > c.C * c.NT) continue;
                     if (d > 1 && (uint64_t) d > nt_max_) continue;
-                    double r = time_candidate(c);
-                    if (r > best_rate * 1.02) {
-                        best_rate = r;
-                        best = c;
-                    }
+                    depths.push_back({ c, time_candidate(c) });
                 }
+                if (!depths.empty()) best = runoff(depths, 0.05);
                 t = best;
                 std::lock_guard<std::mutex> lk(g_tune_mutex);
                 g_tune_cache[key] = t;

@@ -28,9 +28,9 @@ void launch_step_tc(const kparams<float>& p, unsigned grid, size_t smem, cudaStr
         tc::shape<D>::BYTES;
     if (smem < need) smem = need;
     static const cudaError_t attr = cudaFuncSetAttribute(
-        step_kernel<float, 1, LEV, 1, tc::M, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) need);
+        step_kernel_tc<LEV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) need);
     (void) attr;
-    step_kernel<float, 1, LEV, 1, tc::M, true><<<grid, tc::M, smem, s>>>(p);
+    step_kernel_tc<LEV><<<grid, tc::M, smem, s>>>(p);
 }
 
 }  // namespace mbg

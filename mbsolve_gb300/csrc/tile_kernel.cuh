@@ -264,8 +264,8 @@ __device__ __forceinline__ bool tile_steps(
 
 // One launch: every tile advances by nsub steps. TC: 4-6 levels in FP32
 // with the density products of uniform tiles on the tensor cores.
-template<typename T, int ALGO, int LEV, int C, int NT, bool TC = false>
-__global__ void __launch_bounds__(NT, TC ? (LEV <= 4 ? 4 : 3) : 1) step_kernel(const kparams<T> p)
+template<typename T, int ALGO, int LEV, int C, int NT, bool TC>
+__device__ __forceinline__ void step_body(const kparams<T>& p)
 {
     constexpr bool DF = sizeof(T) == 4;
     constexpr int D = density_len<ALGO, LEV>::value;
@@ -477,6 +477,22 @@ __global__ void __launch_bounds__(NT, TC ? (LEV <= 4 ? 4 : 3) : 1) step_kernel(c
             }
         }
     }
+}
+
+// The time-step kernels. The CUDA-core kernels leave the register budget to
+// the compiler (a minimum-blocks hint would raise the 2-level kernels to
+// more registers and one CTA per SM); the tensor-core kernels ask for 3
+// CTAs per SM (4 for 4 levels), which needs the in-place update's budget.
+template<typename T, int ALGO, int LEV, int C, int NT>
+__global__ void __launch_bounds__(NT) step_kernel(const kparams<T> p)
+{
+    step_body<T, ALGO, LEV, C, NT, false>(p);
+}
+
+template<int LEV>
+__global__ void __launch_bounds__(tc::M, LEV <= 4 ? 4 : 3) step_kernel_tc(const kparams<float> p)
+{
+    step_body<float, 1, LEV, 1, tc::M, true>(p);
 }
 
 }  // namespace mbg
