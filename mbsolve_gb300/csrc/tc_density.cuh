@@ -6,11 +6,13 @@
 // t of U and row t of D lands in TMEM lane t, i.e. back in thread t's
 // registers (tcgen05.ld 32x32b). The product runs as tcgen05.mma
 // kind::tf32 (M = 128, N = V rounded up to 16, K = V rounded up to 8) with
-// FP32 accumulation in TMEM, split into high and low TF32 parts for FP32
-// accuracy: Bd u ~ Bd_hi u_hi + Bd_lo u_hi + Bd_hi u_lo (the dropped
-// Bd_lo u_lo is ~2^-22 of the product); a second accumulator takes
-// Bdl u_hi (Bdl = Bd - fl32(Bd), the low-word correction of the FP32
-// kernels). Operands sit in shared memory in the no-swizzle K-major
+// FP32 accumulation in TMEM, split into TF32 parts (rounded to nearest) for
+// FP32 accuracy: Bd u ~ Bd_hi u_hi + Bd_lo u_hi + Bd_hi u_lo (the dropped
+// Bd_lo u_lo is ~2^-22 of the product, and random); a second accumulator
+// takes Bd_rest u_hi, the remainder of Bd + Bdl (Bdl = Bd - fl32(Bd), the
+// low-word correction of the FP32 kernels) beyond Bd_hi + Bd_lo, so the
+// propagator itself is represented to ~2^-33. Operands sit in shared memory
+// in the no-swizzle K-major
 // core-matrix layout (8 rows x 16 bytes per core matrix; 128 bytes between
 // K-adjacent core matrices, K/4 x 128 bytes between 8-row groups).
 //
@@ -137,10 +139,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// Stage the B operands (Bd split into TF32 high and low parts, and Bdl)
-// from the material block in global memory (layout of make_cvr_layout: Bd
-// at FDTD_END, Bdl after it, both V x V row-major). Rows n >= V and
-// columns k >= V are zero. Called by all threads; a barrier must follow.
+// Stage the B operands from the material block in global memory (layout of
+// make_cvr_layout: Bd at FDTD_END, Bdl after it, both V x V row-major):
+// Bd + Bdl = B_hi + B_lo + B_rest with B_hi and B_lo TF32 numbers (rounded
+// to nearest) and B_rest the FP32 remainder. The tensor cores read only a
+// TF32 number's bits, so a B_lo that was not itself a TF32 number would be
+// truncated: a fixed error of ~2^-22 of Bd per material, larger than the
+// Bdl correction. The second accumulator takes B_rest (D1 = A_hi B_rest).
+// Rows n >= V and columns k >= V are zero. Called by all threads; a barrier
+// must follow.
 template<int V>
 __device__ __forceinline__ void stage_b(const ctx& c, const float* mat)
 {
@@ -156,8 +163,9 @@ __device__ __forceinline__ void stage_b(const ctx& c, const float* mat)
             const bool in = n < V && k < V;
             const float b = in ? bd[n * V + k] : 0.0f;
             h[q] = tf32_hi(b);
-            l[q] = b - h[q];
-            dl[q] = in ? bdl[n * V + k] : 0.0f;
+            const float r = b - h[q];           // exact
+            l[q] = tf32_hi(r);
+            dl[q] = (r - l[q]) + (in ? bdl[n * V + k] : 0.0f);
         }
         const uint32_t o = chunk<V>(n, kc);
         st16(c.b_hi + o, h[0], h[1], h[2], h[3]);
@@ -181,7 +189,7 @@ __device__ __forceinline__ void write_row(const ctx& c, const float (&x)[V])
             constexpr int k = kc * 4 + q;
             if constexpr (k < V) {
                 h[q] = tf32_hi(x[k]);
-                l[q] = x[k] - h[q];
+                l[q] = tf32_hi(x[k] - h[q]);  // rounded, not truncated, by the MMA
             } else {
                 h[q] = 0.0f;
                 l[q] = 0.0f;
