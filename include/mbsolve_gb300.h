@@ -175,12 +175,18 @@ typedef struct mbg_grid {
 
 /* Launch shape of the tiled time-step kernel (0 fields = autotuned).
  * cells_per_thread x threads cells form a tile; `depth` time steps run in
- * shared memory/registers per launch (temporal blocking). */
+ * shared memory/registers per launch (temporal blocking). `staging`: 0 =
+ * the tile state is loaded into registers (default), 1 = it is staged in
+ * shared memory by bulk asynchronous (TMA) copies, for the 2-level FP32
+ * solvers (elsewhere 0 is used); the environment variable
+ * MBG_TILE_STAGING=bulk asks for 1 as well. mbg_ensemble_info reports the
+ * staging in use. */
 typedef struct mbg_tuning {
     uint32_t cells_per_thread;
     uint32_t threads;
     uint32_t depth;
     uint32_t launches_per_graph; /* kernel launches captured in one CUDA graph */
+    uint32_t staging;
 } mbg_tuning;
 
 /* ------------------------------------------------------------ entry points */

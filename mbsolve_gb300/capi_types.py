@@ -124,6 +124,7 @@ class mbg_tuning(C.Structure):
         ("threads", C.c_uint32),
         ("depth", C.c_uint32),
         ("launches_per_graph", C.c_uint32),
+        ("staging", C.c_uint32),
     ]
 
 

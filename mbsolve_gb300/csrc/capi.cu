@@ -291,6 +291,7 @@ int mbg_ensemble_info(const mbg_ensemble* e, uint64_t* cells, uint32_t* tiles, m
             t->threads = (uint32_t) u.NT;
             t->depth = (uint32_t) u.depth;
             t->launches_per_graph = (uint32_t) u.graph;
+            t->staging = (uint32_t) e->eng->staging();
         }
     });
 }

@@ -24,7 +24,7 @@ enum : uint32_t {
     STATUS_NONFINITE = 1u,      // a recorded value was NaN or Inf
     STATUS_PRECOMPUTE = 2u,     // the FP64 precompute rejected a material
     STATUS_REGION = 4u,         // a grid point lies in no region
-    STATUS_TC_WAIT = 8u,        // a tensor-core completion wait ran out
+    STATUS_TC_WAIT = 8u,        // a tensor-core or bulk-copy completion wait ran out
 };
 
 // Per-tile work item: one contiguous output range of one run.

@@ -38,16 +38,16 @@ std::vector<kernel_entry<T> >& kernel_registry()
 }
 
 template<typename T>
-bool register_kernel(int algo, int lev, int C, int NT, launch_fn<T> fn)
+bool register_kernel(int algo, int lev, int C, int NT, launch_fn<T> fn, int staging)
 {
-    kernel_registry<T>().push_back(kernel_entry<T>{ algo, lev, C, NT, fn });
+    kernel_registry<T>().push_back(kernel_entry<T>{ algo, lev, C, NT, fn, staging });
     return true;
 }
 
 template std::vector<kernel_entry<float> >& kernel_registry<float>();
 template std::vector<kernel_entry<double> >& kernel_registry<double>();
-template bool register_kernel<float>(int, int, int, int, launch_fn<float>);
-template bool register_kernel<double>(int, int, int, int, launch_fn<double>);
+template bool register_kernel<float>(int, int, int, int, launch_fn<float>, int);
+template bool register_kernel<double>(int, int, int, int, launch_fn<double>, int);
 
 // -------------------------------------------------------------- names
 
@@ -567,6 +567,7 @@ public:
     uint64_t cells() const override { return cells_; }
     uint32_t tiles() const override { return (uint32_t) tiles_host_.size(); }
     tuning tuning_used() const override { return tune_; }
+    int staging() const override { return staging_; }
     void set_timing(bool on) override { timing_ = on; }
     void restart_clock() override { steps_done_ = 0; }
 
@@ -1087,9 +1088,22 @@ private:
     launch_fn<T> find_kernel(int C, int NT) const
     {
         for (const auto& e : kernel_registry<T>())
-            if (e.algo == kind_.algo && e.lev == kind_.N && e.C == C && e.NT == NT) return e.fn;
+            if (e.algo == kind_.algo && e.lev == kind_.N && e.C == C && e.NT == NT && e.staging == staging_)
+                return e.fn;
         return nullptr;
     }
+
+    // MBG_TILE_STAGING=bulk selects the kernels that stage the tile state in
+    // shared memory with bulk (TMA) copies where such kernels exist (2-level
+    // FP32); by default the state goes straight into registers, which
+    // measured faster.
+    static int staging_wanted()
+    {
+        const char* s = std::getenv("MBG_TILE_STAGING");
+        return (s && std::string(s) == "bulk") ? 1 : 0;
+    }
+
+    int staging_ = 0;
 
     kparams<T> params(int in, uint32_t launch_idx, uint32_t nsub, bool record, const unsigned long long* step) const
     {
@@ -1202,7 +1216,7 @@ private:
             for (const char* c = prop.name; *c; c++) s << (std::isalnum((unsigned char) *c) ? *c : '_');
             s << "_" << prop.multiProcessorCount << ":";
         }
-        s << kind_.algo << ":" << kind_.N << ":" << (kind_.fp64 ? 64 : 32) << ":"
+        s << kind_.algo << ":" << kind_.N << ":s" << staging_ << ":" << (kind_.fp64 ? 64 : 32) << ":"
           << (cells_ >> 16) << ":" << runs_.size() << ":" << std::min<uint64_t>(nt_max_, 256);
         return s.str();
     }
@@ -1300,6 +1314,10 @@ private:
 
     void choose_tuning(const mbg_tuning* user)
     {
+        staging_ = 0;
+        if (staging_wanted() || (user && user->staging == 1))
+            for (const auto& e : kernel_registry<T>())
+                if (e.algo == kind_.algo && e.lev == kind_.N && e.staging == 1) staging_ = 1;
         tuning t = default_tuning();
         bool explicit_all = user && user->cells_per_thread && user->threads && user->depth;
         if (user) {
@@ -1328,7 +1346,7 @@ private:
                 // (each stage ends with a run-off of its close contenders)
                 std::vector<std::pair<tuning, double> > shapes;
                 for (const auto& e : kernel_registry<T>()) {
-                    if (e.algo != kind_.algo || e.lev != kind_.N) continue;
+                    if (e.algo != kind_.algo || e.lev != kind_.N || e.staging != staging_) continue;
                     tuning c = t;
                     c.C = e.C;
                     c.NT = e.NT;

@@ -87,6 +87,7 @@ public:
     virtual uint64_t cells() const = 0;
     virtual uint32_t tiles() const = 0;
     virtual tuning tuning_used() const = 0;
+    virtual int staging() const = 0;  // 0: registers, 1: bulk-copy staging
     virtual void set_timing(bool on) = 0;
     virtual void kernel_time(uint64_t* launches, double* ms, bool reset) = 0;
     virtual uint32_t status() = 0;
@@ -127,12 +128,13 @@ template<typename T>
 struct kernel_entry {
     int algo, lev, C, NT;
     launch_fn<T> fn;
+    int staging;  // 0: tile state loaded into registers, 1: bulk-copy (TMA) staging
 };
 
 template<typename T>
 std::vector<kernel_entry<T> >& kernel_registry();
 
 template<typename T>
-bool register_kernel(int algo, int lev, int C, int NT, launch_fn<T> fn);
+bool register_kernel(int algo, int lev, int C, int NT, launch_fn<T> fn, int staging = 0);
 
 }  // namespace mbg

@@ -18,6 +18,18 @@ void launch_step(const kparams<T>& p, unsigned grid, size_t smem, cudaStream_t s
     step_kernel<T, ALGO, LEV, C, NT><<<grid, NT, smem, s>>>(p);
 }
 
+// 2-level FP32 with bulk-copy staging: room for the staged planes after the
+// coefficients
+template<int C, int NT>
+void launch_step_bulk(const kparams<float>& p, unsigned grid, size_t smem, cudaStream_t s)
+{
+    const size_t need = ((smem + 127) & ~(size_t) 127) + 128 + bulk::bytes<3>(C * NT);
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(step_kernel_bulk<C, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) need);
+    (void) attr;
+    step_kernel_bulk<C, NT><<<grid, NT, need, s>>>(p);
+}
+
 // FP32 coherence-vector kernels for 4-6 levels with the density products
 // of uniform tiles on the tensor cores (128 threads, one point each).
 template<int LEV>
@@ -38,6 +50,10 @@ void launch_step_tc(const kparams<float>& p, unsigned grid, size_t smem, cudaStr
 #define MBG_REG_CVR_TC(LEV)                                                       \
     static const bool MBG_CAT(mbg_reg_, __LINE__) = ::mbg::register_kernel<float>( \
         ::mbg::ALGO_CVR, LEV, 1, ::mbg::tc::M, &::mbg::launch_step_tc<LEV>);
+
+#define MBG_REG_CVR2_BULK(C, NT)                                                  \
+    static const bool MBG_CAT(mbg_reg_, __LINE__) = ::mbg::register_kernel<float>( \
+        ::mbg::ALGO_CVR, 2, C, NT, &::mbg::launch_step_bulk<C, NT>, 1);
 
 #define MBG_CAT2(a, b) a##b
 #define MBG_CAT(a, b) MBG_CAT2(a, b)

@@ -10,6 +10,7 @@
 
 #include "kernels.cuh"
 #include "tc_density.cuh"
+#include "bulk_stage.cuh"
 
 namespace mbg {
 
@@ -264,7 +265,7 @@ __device__ __forceinline__ bool tile_steps(
 
 // One launch: every tile advances by nsub steps. TC: 4-6 levels in FP32
 // with the density products of uniform tiles on the tensor cores.
-template<typename T, int ALGO, int LEV, int C, int NT, bool TC>
+template<typename T, int ALGO, int LEV, int C, int NT, bool TC, bool BULK = false>
 __device__ __forceinline__ void step_body(const kparams<T>& p)
 {
     constexpr bool DF = sizeof(T) == 4;
@@ -319,24 +320,58 @@ __device__ __forceinline__ void step_body(const kparams<T>& p)
     T R[C][DD];
     T Rl[C][DD];  // FP32 coherence vector: low words
     int32_t M[C];
-    load_cells<T, C>(E, p.Ein, g0);
-    load_cells<T, C>(H, p.Hin, g0);
-    load_cells<T, C>(P, p.Pin, g0);
-    if constexpr (DF) {
-        load_cells<T, C>(El, p.Elin, g0);
-        load_cells<T, C>(Hl, p.Hlin, g0);
-    }
-    if constexpr (D > 0) {
+    // BULK: the tile's state planes are staged in shared memory with bulk
+    // asynchronous copies (TMA); otherwise they load straight into registers
+    static_assert(!BULK || bulk::enabled<T, ALGO, LEV, TC>(), "bulk staging: 2-level FP32 only");
+    __shared__ __align__(8) uint64_t bulk_mbar;
+    uint32_t bulk_s = 0;
+    float* bulk_g = nullptr;
+    if constexpr (BULK) {
+        const uint32_t sraw = (uint32_t) __cvta_generic_to_shared(smem_raw);
+        bulk_s = (sraw + (uint32_t) (p.mstage * sizeof(T)) + 127u) & ~127u;
+        bulk_g = reinterpret_cast<float*>(smem_raw + (bulk_s - sraw));
+        const uint64_t gt = (uint64_t) ((int64_t) rd.offset + (int64_t) td.out_start - (int64_t) p.halo);
+        const bool ok = bulk::load<D, NT * C>(p, gt, (uint32_t) __cvta_generic_to_shared(&bulk_mbar), bulk_s);
+        if (!ok) {
+            if (threadIdx.x == 0) atomicOr(p.status, STATUS_TC_WAIT);
+            return;
+        }
+        const float* mine = bulk_g + threadIdx.x * C;
+        bulk::take<C>(E, mine, 0, NT * C);
+        bulk::take<C>(H, mine, 1, NT * C);
+        bulk::take<C>(P, mine, 2, NT * C);
+        bulk::take<C>(El, mine, 3, NT * C);
+        bulk::take<C>(Hl, mine, 4, NT * C);
 #pragma unroll
         for (int v = 0; v < D; v++) {
             T tmp[C];
-            load_cells<T, C>(tmp, p.Din + (uint64_t) v * p.plane, g0);
+            bulk::take<C>(tmp, mine, 5 + v, NT * C);
 #pragma unroll
             for (int j = 0; j < C; j++) R[j][v] = tmp[j];
-            if constexpr (DFD) {
-                load_cells<T, C>(tmp, p.Din + (uint64_t) (D + v) * p.plane, g0);
+            bulk::take<C>(tmp, mine, 5 + D + v, NT * C);
 #pragma unroll
-                for (int j = 0; j < C; j++) Rl[j][v] = tmp[j];
+            for (int j = 0; j < C; j++) Rl[j][v] = tmp[j];
+        }
+    } else {
+        load_cells<T, C>(E, p.Ein, g0);
+        load_cells<T, C>(H, p.Hin, g0);
+        load_cells<T, C>(P, p.Pin, g0);
+        if constexpr (DF) {
+            load_cells<T, C>(El, p.Elin, g0);
+            load_cells<T, C>(Hl, p.Hlin, g0);
+        }
+        if constexpr (D > 0) {
+#pragma unroll
+            for (int v = 0; v < D; v++) {
+                T tmp[C];
+                load_cells<T, C>(tmp, p.Din + (uint64_t) v * p.plane, g0);
+#pragma unroll
+                for (int j = 0; j < C; j++) R[j][v] = tmp[j];
+                if constexpr (DFD) {
+                    load_cells<T, C>(tmp, p.Din + (uint64_t) (D + v) * p.plane, g0);
+#pragma unroll
+                    for (int j = 0; j < C; j++) Rl[j][v] = tmp[j];
+                }
             }
         }
     }
@@ -455,6 +490,29 @@ __device__ __forceinline__ void step_body(const kparams<T>& p)
         }
     }
 
+    if constexpr (BULK) {
+        // every thread puts its cells back into the staged planes; one thread
+        // writes the tile's output range to global memory with bulk copies
+        float* mine = bulk_g + threadIdx.x * C;
+        bulk::give<C>(E, mine, 0, NT * C);
+        bulk::give<C>(H, mine, 1, NT * C);
+        bulk::give<C>(P, mine, 2, NT * C);
+        bulk::give<C>(El, mine, 3, NT * C);
+        bulk::give<C>(Hl, mine, 4, NT * C);
+#pragma unroll
+        for (int v = 0; v < D; v++) {
+            T tmp[C];
+#pragma unroll
+            for (int j = 0; j < C; j++) tmp[j] = R[j][v];
+            bulk::give<C>(tmp, mine, 5 + v, NT * C);
+#pragma unroll
+            for (int j = 0; j < C; j++) tmp[j] = Rl[j][v];
+            bulk::give<C>(tmp, mine, 5 + D + v, NT * C);
+        }
+        bulk::store<D, NT * C>(p, (uint64_t) rd.offset + (uint64_t) td.out_start, (uint32_t) td.out_len,
+                               bulk_s + (uint32_t) (p.halo * sizeof(float)));
+        return;
+    }
     const int64_t lo = td.out_start, hi = (int64_t) td.out_start + td.out_len;
     store_cells<T, C>(E, p.Eout, g0, l0, lo, hi);
     store_cells<T, C>(H, p.Hout, g0, l0, lo, hi);
@@ -493,6 +551,15 @@ template<int LEV>
 __global__ void __launch_bounds__(tc::M, LEV <= 4 ? 4 : 3) step_kernel_tc(const kparams<float> p)
 {
     step_body<float, 1, LEV, 1, tc::M, true>(p);
+}
+
+// 2-level FP32 kernels with bulk-copy (TMA) staging of the tile state; not
+// the default (measured slower on this issue-bound kernel), selected by
+// MBG_TILE_STAGING=bulk
+template<int C, int NT>
+__global__ void __launch_bounds__(NT) step_kernel_bulk(const kparams<float> p)
+{
+    step_body<float, 1, 2, C, NT, false, true>(p);
 }
 
 }  // namespace mbg

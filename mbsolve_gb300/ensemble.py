@@ -69,7 +69,8 @@ class ensemble:
                                                 C.byref(tiles), C.byref(t)))
         return dict(cells=cells.value, tiles=tiles.value,
                     cells_per_thread=t.cells_per_thread, threads=t.threads,
-                    depth=t.depth, launches_per_graph=t.launches_per_graph)
+                    depth=t.depth, launches_per_graph=t.launches_per_graph,
+                    staging=t.staging)
 
     def results(self, run):
         out = []
@@ -162,8 +163,12 @@ class ensemble:
         self.close()
 
 
-def tuning(cells_per_thread=0, threads=0, depth=0, launches_per_graph=0):
+def tuning(cells_per_thread=0, threads=0, depth=0, launches_per_graph=0,
+           staging=0):
+    """Launch shape (0 = autotuned); staging 1 = bulk-copy (TMA) staging of
+    the tile state (2-level FP32)."""
     t = T.mbg_tuning()
+    t.staging = staging
     t.cells_per_thread = cells_per_thread
     t.threads = threads
     t.depth = depth
