@@ -181,3 +181,42 @@ def test_errors_reported_like_reference(native):
     dev2, sce2 = setups.sit_2lvl(64, 10)
     with pytest.raises(RuntimeError, match="does not match"):
         solvergpu.solver_gpu_fdtd(dev2, sce2, "gpu-fdtd-3lvl-cvr-rodr-fp32")
+
+
+def _mixed_3lvl():
+    """A 0-D run, 1-D runs of very different lengths and step counts, and a
+    two-point run, all 3-level."""
+    return [("song2005", dict(num_timesteps=3000)),
+            ("lambda_3lvl", dict(num_gridpoints=2000, num_timesteps=1500)),
+            ("random_nlvl", dict(N=3, num_gridpoints=500, num_timesteps=800,
+                                 seed=4)),
+            ("random_nlvl", dict(N=3, num_gridpoints=2, num_timesteps=300,
+                                 seed=5))]
+
+
+@pytest.mark.parametrize("algo", ["cvr-rodr", "reg-cayley"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_mixed_ensemble_equals_single_runs(native, algo, prec):
+    """Runs of every shape in one launch sequence give exactly the single
+    runs' results (and, in FP64, the oracle's)."""
+    from mbsolve_gb300 import ensemble
+    name = "gpu-fdtd-3lvl-%s-%s" % (algo, prec)
+    specs = _mixed_3lvl()
+    mb.material.clear_library()
+    pairs = [helpers.build_setup({"setup": s, "kw": kw}) for s, kw in specs]
+    ens = ensemble.ensemble(name, pairs)
+    ens.run()
+    assert ens.status() == 0
+    for i, (s, kw) in enumerate(specs):
+        mb.material.clear_library()
+        dev, sce = helpers.build_setup({"setup": s, "kw": kw})
+        _, single = helpers.gpu_results(name, dev, sce)
+        got = [r.as_array() for r in ens.results(i)]
+        for a, b in zip(got, single):
+            assert np.array_equal(a, b), (s, i)
+        if prec == "fp64":
+            mb.material.clear_library()
+            dev, sce = helpers.build_setup({"setup": s, "kw": kw})
+            _, orc = helpers.oracle_results(algo, 3, dev, sce)
+            for a, b in zip(got, orc):
+                _check(a, b, 1e-9, ("mixed", s, i))
