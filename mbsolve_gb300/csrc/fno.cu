@@ -42,6 +42,7 @@ constexpr int A_BYTES = BM * BK * 2;
 constexpr int B_BYTES = BN * BK * 2;
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 128;  // + alignment slack
+static_assert(BM * (BN + 1) * 4 <= STAGES * STAGE_BYTES, "epilogue tile must fit the stages");
 constexpr int TMEM_COLS = 64;    // power of two >= 32
 constexpr uint32_t LBO = 128;    // K-direction core-matrix stride (bytes)
 constexpr uint32_t SBO = 1024;   // M/N-direction 8-row-group stride (bytes)
@@ -372,36 +373,46 @@ __global__ void __launch_bounds__(NTH) gemm_kernel(const gemm_params p)
     fence_after();
 
     if (ok) {
-        const int row = m0 + warp * 32 + lane;
-        const bool rv = row < p.m;
+        // The accumulator comes out of TMEM one row per thread; it goes
+        // through shared memory (the stages are free: every MMA has
+        // completed) so that the epilogue reads and writes C, pre and gate
+        // along their contiguous dimension (a row per thread would make a
+        // warp's every access touch 32 rows).
+        constexpr int LD = BN + 1;  // odd stride: conflict-free both ways
+        float* tile = reinterpret_cast<float*>(smem_raw + (base - smem_u32(smem_raw)));
+        const int r0 = warp * 32 + lane;
 #pragma unroll 1
         for (int cb = 0; cb < BN / 16; cb++) {
             float acc[16];
             tmem_ld16(tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) (cb * 16), acc);
-            if (!rv) continue;
-            const int64_t rowoff = (int64_t) z * p.c_sz + (int64_t) row * p.c_sm;
 #pragma unroll
-            for (int i = 0; i < 16; i++) {
-                const int col = n0 + cb * 16 + i;
-                if (col >= p.n) continue;
-                const int64_t off = rowoff + (int64_t) col * p.c_sn;
-                float v = p.alpha * acc[i];
-                if (p.mode == MBG_GEMM_ATOMIC) {
-                    atomicAdd(reinterpret_cast<float*>(p.c) + off, v);
-                    continue;
-                }
-                if (p.mode == MBG_GEMM_ACCUM) v += ld_elem(p.c, p.c_type, off);
-                if (p.bias) v += p.bias[col];
-                if (p.pre) p.pre[off] = v;
-                if (p.act == MBG_ACT_GELU)
-                    v = gelu(v);
-                else if (p.act == MBG_ACT_GELU_BWD)
-                    v *= gelu_grad(p.gate[off]);
-                if (p.c_type == MBG_BF16)
-                    reinterpret_cast<__nv_bfloat16*>(p.c)[off] = __float2bfloat16_rn(v);
-                else
-                    reinterpret_cast<float*>(p.c)[off] = v;
+            for (int i = 0; i < 16; i++) tile[r0 * LD + cb * 16 + i] = acc[i];
+        }
+        __syncthreads();
+        const bool rows_fast = p.c_sn != 1 && p.c_sm == 1;
+#pragma unroll 1
+        for (int e = tid; e < BM * BN; e += NTH) {
+            const int r = rows_fast ? e % BM : e / BN;
+            const int cc = rows_fast ? e / BM : e % BN;
+            const int row = m0 + r, col = n0 + cc;
+            if (row >= p.m || col >= p.n) continue;
+            const int64_t off = (int64_t) z * p.c_sz + (int64_t) row * p.c_sm + (int64_t) col * p.c_sn;
+            float v = p.alpha * tile[r * LD + cc];
+            if (p.mode == MBG_GEMM_ATOMIC) {
+                atomicAdd(reinterpret_cast<float*>(p.c) + off, v);
+                continue;
             }
+            if (p.mode == MBG_GEMM_ACCUM) v += ld_elem(p.c, p.c_type, off);
+            if (p.bias) v += p.bias[col];
+            if (p.pre) p.pre[off] = v;
+            if (p.act == MBG_ACT_GELU)
+                v = gelu(v);
+            else if (p.act == MBG_ACT_GELU_BWD)
+                v *= gelu_grad(p.gate[off]);
+            if (p.c_type == MBG_BF16)
+                reinterpret_cast<__nv_bfloat16*>(p.c)[off] = __float2bfloat16_rn(v);
+            else
+                reinterpret_cast<float*>(p.c)[off] = v;
         }
     }
     if (fail_sh && tid == 0) atomicOr(p.status, ST_WAIT);
