@@ -333,36 +333,33 @@ __device__ __forceinline__ void row_dot(const CF& c, const T (&x)[V], T& s, T& s
     }
 }
 
-// Coherence-vector update in the plane basis (see precompute.cuh):
-// w = u + (Bd u + k); rotate each plane by theta_k dt e; u = w + (Bd w + k);
-// P = p0 + g . u.
+// Coherence-vector step in the plane basis, on the state v kept one half
+// step ahead (see cvr_layout in precompute.cuh): rotate each plane by
+// theta_k dt e; v = v + (Bd v + k); P = p0 + g . v.
 template<typename T, int V, class CF>
 __device__ __forceinline__ void cvr_update(T (&u)[V], T e, T& pout, const CF& cf)
 {
-    T w[V];
-    const auto c1 = cf.pass();
-    static_for<0, V>([&](auto I) {
-        constexpr int i = decltype(I)::value;
-        T s = c1.k(i), sl = T(0);
-        row_dot<false, i>(c1, u, s, sl);
-        w[i] = u[i] + s;
-    });
+    const auto c = cf.pass();
     static_for<0, V / 2>([&](auto K) {
         constexpr int k = decltype(K)::value;
         T sn, s2;
-        rot_coeffs<T>(c1.th(k) * e, sn, s2);
-        T a = w[2 * k], b = w[2 * k + 1];
-        w[2 * k] = a - fma(s2, a, sn * b);
-        w[2 * k + 1] = b + fma(sn, a, -s2 * b);
+        rot_coeffs<T>(c.th(k) * e, sn, s2);
+        T a = u[2 * k], b = u[2 * k + 1];
+        u[2 * k] = a - fma(s2, a, sn * b);
+        u[2 * k + 1] = b + fma(sn, a, -s2 * b);
     });
-    const auto c2 = cf.pass();
-    T pp = c2.p0();
+    T s[V];
     static_for<0, V>([&](auto I) {
         constexpr int i = decltype(I)::value;
-        T s = c2.k(i), sl = T(0);
-        row_dot<false, i>(c2, w, s, sl);
-        u[i] = w[i] + s;
-        pp = fma(c2.g(i), u[i], pp);
+        T sl = T(0);
+        s[i] = c.k(i);
+        row_dot<false, i>(c, u, s[i], sl);
+    });
+    T pp = c.p0();
+    static_for<0, V>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        u[i] += s[i];
+        pp = fma(c.g(i), u[i], pp);
     });
     pout = pp;
 }
@@ -417,44 +414,37 @@ struct cvr_coef_reg {
     __device__ __forceinline__ const cvr_coef_reg& pass() const { return *this; }  // stays in registers
 };
 
-// The same update in FP32 with u = uh + ul: the corrections are computed in
-// FP32 from the high words and accumulated error-free; the low words take
-// the rounding errors and the Bdl contribution; one renormalisation per
-// step.
+// The same step in FP32 with v = uh + ul: the rotation and the correction
+// are computed in FP32 from the high words and accumulated error-free; the
+// low words take the rounding errors and the Bdl contribution; one
+// renormalisation per step.
 template<int V, class CF>
 __device__ __forceinline__ void cvr_update_df(float (&uh)[V], float (&ul)[V], float e, float& pout, const CF& cf)
 {
-    float wh[V], wl[V];
-    const auto c1 = cf.pass();
-    static_for<0, V>([&](auto I) {
-        constexpr int i = decltype(I)::value;
-        float c = c1.k(i), cl = 0.0f;
-        row_dot<true, i>(c1, uh, c, cl);
-        wh[i] = uh[i];
-        wl[i] = ul[i];
-        df_acc(wh[i], wl[i], c, cl);
-    });
+    const auto c = cf.pass();
     static_for<0, V / 2>([&](auto K) {
         constexpr int k = decltype(K)::value;
         float sn, s2;
-        rot_coeffs<float>(c1.th(k) * e, sn, s2);
-        const float a = wh[2 * k], b = wh[2 * k + 1];
+        rot_coeffs<float>(c.th(k) * e, sn, s2);
+        const float a = uh[2 * k], b = uh[2 * k + 1];
         const float da = -fmaf(s2, a, sn * b);
         const float db = fmaf(sn, a, -s2 * b);
-        df_acc(wh[2 * k], wl[2 * k], da, 0.0f);
-        df_acc(wh[2 * k + 1], wl[2 * k + 1], db, 0.0f);
+        df_acc(uh[2 * k], ul[2 * k], da, 0.0f);
+        df_acc(uh[2 * k + 1], ul[2 * k + 1], db, 0.0f);
     });
-    const auto c2 = cf.pass();
-    float pp = c2.p0();
+    float s[V], sl[V];
     static_for<0, V>([&](auto I) {
         constexpr int i = decltype(I)::value;
-        float c = c2.k(i), cl = 0.0f;
-        row_dot<true, i>(c2, wh, c, cl);
-        uh[i] = wh[i];
-        ul[i] = wl[i];
-        df_acc(uh[i], ul[i], c, cl);
+        s[i] = c.k(i);
+        sl[i] = 0.0f;
+        row_dot<true, i>(c, uh, s[i], sl[i]);
+    });
+    float pp = c.p0();
+    static_for<0, V>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        df_acc(uh[i], ul[i], s[i], sl[i]);
         df_renorm(uh[i], ul[i]);
-        pp = fmaf(c2.g(i), uh[i], fmaf(c2.g(i), ul[i], pp));
+        pp = fmaf(c.g(i), uh[i], fmaf(c.g(i), ul[i], pp));
     });
     pout = pp;
 }

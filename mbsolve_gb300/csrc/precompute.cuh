@@ -10,20 +10,24 @@
 //     d1 = A1 (d + d_in) - d_in,  d2 = A2(e) d1,  d = A1 (d2 + d_in) - d_in
 // with A1 = exp(M dt/2) and A2(e) = exp(e dt U), U skew-symmetric, A2 built
 // from the real-Schur planes of U. Here the state is the same vector in the
-// basis Q of those planes, u = Q^T d. With B = Q^T A1 Q = I + Bd,
-// F = A1 - I and the small constant k = Q^T F d_in (A1 d + F d_in is the
-// reference's first half step):
-//     w = u + (Bd u + k);  w <- R(e) w;  u = w + (Bd w + k)
-// where R(e) is block-diagonal with a 2x2 rotation by theta_k e dt per plane
-// and the identity on the null space of U: two V x V products and V/2 plane
-// rotations per point and step instead of forming A2. The polarisation
-// current p_t = M_CP v^T (M d + d_eq) becomes g^T u + p0 with
-// g = M_CP Q^T M^T v and p0 = M_CP v^T d_eq. Every stage adds a small
-// correction to a vector of norm about 1; Bd comes from exp(X) - I computed
-// directly. The FP32 kernels keep u as a float pair (hi + lo), add the
-// corrections with TwoSum and add Bdl = Bd - fl32(Bd) into the low word:
-// otherwise the FP32 rounding of Bd acts as a systematic shift of the
-// transition frequency.
+// basis Q of those planes, u = Q^T d. With F = A1 - I and the small
+// constant kh = Q^T F d_in (A1 d + F d_in is the reference's first half
+// step), one step is
+//     w = u + (Bh u + kh);  w <- R(e) w;  u = w + (Bh w + kh)
+// with Bh = Q^T F Q and R(e) block-diagonal with a 2x2 rotation by
+// theta_k e dt per plane and the identity on the null space of U: V/2 plane
+// rotations per point instead of forming A2. The second half step of one
+// step and the first of the next merge into one full step, so the kernels
+// keep v = u + (Bh u + kh) and do one product per step (cvr_layout):
+//     v <- R(e) v;  v = v + (Bd v + k),  Bd = Q^T (exp(M dt) - I) Q.
+// The polarisation current p_t = M_CP v_dip^T (M d + d_eq) is g^T u + p0
+// with g = M_CP Q^T M^T v_dip and p0 = M_CP v_dip^T d_eq, composed with
+// u = A1^-1 (v - kh) into a row on v. Every stage adds a small correction
+// to a vector of norm about 1; Bd comes from exp(X) - I computed directly.
+// The FP32 kernels keep v as a float pair (hi + lo), add the corrections
+// with TwoSum and add Bdl = Bd - fl32(Bd) into the low word: otherwise the
+// FP32 rounding of Bd acts as a systematic shift of the transition
+// frequency.
 //
 // Planes of U: U is real skew-symmetric, so i U is complex Hermitian with
 // eigenvalues +-theta_k; an eigenvector a + i b for +theta gives the
@@ -100,11 +104,24 @@ enum : int {
 };
 
 // Constant block of one material for the coherence-vector kernels.
+//
+// The reference's step (rodr.hpp:234-268) is, in the plane basis u = Q^T d,
+//   u <- A u + kh;  u <- R(e) u;  u <- A u + kh
+// with A = exp(M dt/2) and kh = (A - I) d_in. Two consecutive steps meet
+// in A (A u + kh) + kh = A^2 u + (A^2 - I) d_in: the kernels therefore keep
+// the state one half step ahead, v = A u + kh, and advance it by
+//   v <- R(e) v;  v <- v + (Bd v + k)
+// with Bd = A^2 - I = Q^T (exp(M dt) - I) Q and k = Q^T (exp(M dt) - I) d_in:
+// one matrix product per step instead of two. u = A^-1 (v - kh) is never
+// formed: P = p0 + g . v and the records' rows (inv, pop) are composed with
+// A^-1 and kh here, and the initial state z0 is v0 = A u0 + kh. Bh and kh
+// (the half step) are kept after Q for inspection.
 struct cvr_layout {
     int N, V, KP;
     int a, b, cH, gam, has_qm, p0, nplanes;
     int Bd, Bdl, k, g, thdt, z0, inv, inv_c, pop, pop_c;
     int Q;       // the plane basis (inspection only; kernels stop before it)
+    int Bh, kh;  // the half step (inspection only)
     int stage;   // leading part a kernel stages in shared memory
     int stride;
 };
@@ -146,6 +163,10 @@ MBG_HD cvr_layout make_cvr_layout(int N)
     L.stage = (o + 3) & ~3;
     L.Q = L.stage;
     o = L.Q + L.V * L.V;
+    L.Bh = o;
+    o += L.V * L.V;
+    L.kh = o;
+    o += L.V;
     L.stride = (o + 3) & ~3;
     return L;
 }
@@ -784,54 +805,96 @@ MBG_HD int cvr_precompute(const mat_in& m, int Nsolver, double* ws, double* out)
     }
 
     for (int i = 0; i < V * V; i++) out[L.Q + i] = Q[i];
-    // Bd = Q^T F Q   (= Q^T A1 Q - I)
-    for (int i = 0; i < V; i++)
-        for (int j = 0; j < V; j++) {
+    // out[o] = Q^T X Q for X (V x V, original basis); H1 is scratch
+    auto to_planes = [&](const double* X, double* dst) {
+        for (int i = 0; i < V; i++)
+            for (int j = 0; j < V; j++) {
+                double s = 0.0;
+                for (int k = 0; k < V; k++) s += X[i * V + k] * Q[k * V + j];
+                H1[i * V + j] = s;  // X Q
+            }
+        for (int i = 0; i < V; i++)
+            for (int j = 0; j < V; j++) {
+                double s = 0.0;
+                for (int k = 0; k < V; k++) s += Q[k * V + i] * H1[k * V + j];
+                dst[i * V + j] = s;
+            }
+    };
+    // Q^T X d_in
+    auto drive = [&](const double* X, double* dst) {
+        for (int i = 0; i < V; i++) {
             double s = 0.0;
-            for (int k = 0; k < V; k++) s += F[i * V + k] * Q[k * V + j];
-            H1[i * V + j] = s;  // F Q
+            for (int j = 0; j < V; j++) s += X[i * V + j] * d_in[j];
+            t2[i] = s;
         }
-    for (int i = 0; i < V; i++)
-        for (int j = 0; j < V; j++) {
+        for (int k = 0; k < V; k++) {
             double s = 0.0;
-            for (int k = 0; k < V; k++) s += Q[k * V + i] * H1[k * V + j];
-            out[L.Bd + i * V + j] = s;
-            out[L.Bdl + i * V + j] = s - (double) (float) s;
+            for (int i = 0; i < V; i++) s += Q[i * V + k] * t2[i];
+            dst[k] = s;
         }
-    // k = Q^T (A1 - I) d_in ; g = M_CP Q^T M^T v ; p0 = M_CP v^T d_eq
+    };
+    // half step: Bh = Q^T (exp(M dt/2) - I) Q, kh = Q^T (exp(M dt/2) - I) d_in
+    double* Bh = out + L.Bh;
+    double* kh = out + L.kh;
+    to_planes(F, Bh);
+    drive(F, kh);
+    // full step: Bd = Q^T (exp(M dt) - I) Q, k = Q^T (exp(M dt) - I) d_in
+    for (int i = 0; i < V * V; i++) H2[i] = M[i] * m.dt;
+    expm_minus_identity(H2, E1, V, W);
+    to_planes(E1, out + L.Bd);
+    for (int i = 0; i < V * V; i++) out[L.Bdl + i] = out[L.Bd + i] - (double) (float) out[L.Bd + i];
+    drive(E1, out + L.k);
+    // Bi = A^-1 - I = Q^T (exp(-M dt/2) - I) Q
+    for (int i = 0; i < V * V; i++) H2[i] = -M[i] * m.dt / 2;
+    expm_minus_identity(H2, E2, V, W);
+    double* Bi = E1;
+    to_planes(E2, Bi);
+    // a row r on u becomes r (I + Bi) on v with constant -r (I + Bi) kh
+    auto compose = [&](double* r, double& c) {
+        for (int j = 0; j < V; j++) {
+            double s = r[j];
+            for (int i = 0; i < V; i++) s += r[i] * Bi[i * V + j];
+            t1[j] = s;
+        }
+        for (int j = 0; j < V; j++) {
+            r[j] = t1[j];
+            c -= t1[j] * kh[j];
+        }
+    };
+    // P = p0 + g . u with g = M_CP Q^T M^T v_dip, p0 = M_CP v_dip . d_eq
+    // (rodr.hpp:258-266)
     for (int j = 0; j < V; j++) {
         double s = 0.0;
         for (int i = 0; i < V; i++) s += M[i * V + j] * v_dip[i];
-        t1[j] = s;  // (M^T v)_j
-    }
-    for (int i = 0; i < V; i++) {
-        double s = 0.0;
-        for (int j = 0; j < V; j++) s += F[i * V + j] * d_in[j];
-        t2[i] = s;  // F d_in
+        t2[j] = s;  // (M^T v)_j
     }
     double p0 = 0.0;
     for (int i = 0; i < V; i++) p0 += v_dip[i] * d_eq[i];
-    out[L.p0] = M_CP * p0;
     for (int k = 0; k < V; k++) {
-        double sk = 0.0, sg = 0.0;
-        for (int i = 0; i < V; i++) {
-            sk += Q[i * V + k] * t2[i];
-            sg += Q[i * V + k] * t1[i];
-        }
-        out[L.k + k] = sk;
+        double sg = 0.0;
+        for (int i = 0; i < V; i++) sg += Q[i * V + k] * t2[i];
         out[L.g + k] = M_CP * sg;
     }
-    // initial state u0 = Q^T d0
+    p0 *= M_CP;
+    compose(out + L.g, p0);
+    out[L.p0] = p0;
+    // initial state v0 = A u0 + kh, u0 = Q^T d0
     initial_coherence_vector(m, d0);
     for (int k = 0; k < V; k++) {
         double s = 0.0;
         for (int i = 0; i < V; i++) s += Q[i * V + k] * d0[i];
-        out[L.z0 + k] = s;
+        t2[k] = s;
+    }
+    for (int i = 0; i < V; i++) {
+        double s = t2[i] + kh[i];
+        for (int j = 0; j < V; j++) s += Bh[i * V + j] * t2[j];
+        out[L.z0 + i] = s;
     }
     // observables: d = Q u
     int w0 = N * (N - 1);
     for (int k = 0; k < V; k++) out[L.inv + k] = Q[w0 * V + k];
     out[L.inv_c] = 0.0;
+    compose(out + L.inv, out[L.inv_c]);
     for (int mm = 0; mm < N; mm++) {
         for (int k = 0; k < V; k++) out[L.pop + mm * V + k] = 0.0;
         for (int i = 0; i < N - 1; i++) {
@@ -840,6 +903,7 @@ MBG_HD int cvr_precompute(const mat_in& m, int Nsolver, double* ws, double* out)
                 out[L.pop + mm * V + k] += w * Q[(w0 + i) * V + k];
         }
         out[L.pop_c + mm] = population_const(N, mm);
+        compose(out + L.pop + mm * V, out[L.pop_c + mm]);
     }
     return 0;
 }

@@ -1,8 +1,9 @@
-// Tensor-core form of the coherence-vector half steps for 4 to 6 levels
+// Tensor-core form of the coherence-vector step for 4 to 6 levels
 // (FP32 kernels, uniform tiles, 128 points per CTA, one per thread).
 //
-// Each half step w = u + (Bd u + k) is, over the CTA's 128 points, the
-// product D[128 x V] = U[128 x V] Bd^T: thread t's coherence vector is row
+// Each step's correction Bd v + k (after the field rotation; see
+// cvr_layout) is, over the CTA's 128 points, the product
+// D[128 x V] = U[128 x V] Bd^T: thread t's coherence vector is row
 // t of U and row t of D lands in TMEM lane t, i.e. back in thread t's
 // registers (tcgen05.ld 32x32b). The product runs as tcgen05.mma
 // kind::tf32 (M = 128, N = V rounded up to 16, K = V rounded up to 8) with
@@ -270,21 +271,11 @@ struct coef_small {
     }
 };
 
-// The FP32 coherence-vector update of cvr_update_df with the two matrix
-// products on the tensor cores. The products read their own copy of the
-// vector (shared memory), so the registers are updated in place. All
-// threads of the CTA call it (threads without a point pass zeros and
-// discard the result).
+// Rotation of the planes of v = uh + ul by theta_k dt e (the first part of
+// cvr_update_df).
 template<int V, class CF>
-__device__ __forceinline__ bool cvr_update_df_tc(
-    ctx& c, float (&uh)[V], float (&ul)[V], float e, float& pout, const CF& cf)
+__device__ __forceinline__ void rotate_df(float (&uh)[V], float (&ul)[V], float e, const CF& cf)
 {
-    write_row<V>(c, uh);
-    if (!product<V>(c)) return false;
-    consume_row<V>(c, [&](auto I, float d, float dl) {
-        constexpr int i = decltype(I)::value;
-        df_acc(uh[i], ul[i], cf.k(i) + d, dl);
-    });
     static_for<0, V / 2>([&](auto KI) {
         constexpr int k = decltype(KI)::value;
         float sn, s2;
@@ -295,7 +286,18 @@ __device__ __forceinline__ bool cvr_update_df_tc(
         df_acc(uh[2 * k], ul[2 * k], da, 0.0f);
         df_acc(uh[2 * k + 1], ul[2 * k + 1], db, 0.0f);
     });
-    fence_before();   // the reads of D above precede the next product's MMAs
+}
+
+// The FP32 coherence-vector step of cvr_update_df with its matrix product
+// on the tensor cores. The product reads its own copy of the vector
+// (shared memory), so the registers are updated in place. All threads of
+// the CTA call it (threads without a point pass zeros and discard the
+// result).
+template<int V, class CF>
+__device__ __forceinline__ bool cvr_update_df_tc(
+    ctx& c, float (&uh)[V], float (&ul)[V], float e, float& pout, const CF& cf)
+{
+    rotate_df<V>(uh, ul, e, cf);
     write_row<V>(c, uh);
     if (!product<V>(c)) return false;
     float pp = cf.p0();
@@ -306,52 +308,37 @@ __device__ __forceinline__ bool cvr_update_df_tc(
         pp = fmaf(cf.g(i), uh[i], fmaf(cf.g(i), ul[i], pp));
     });
     pout = pp;
-    fence_before();
+    fence_before();   // the reads of D above precede the next product's MMAs
     return true;
 }
 
-// The same update on the CUDA cores with the point's own coefficients
+// The same step on the CUDA cores with the point's own coefficients
 // (mixed-material tiles of the tensor-core kernel): the vector goes to this
-// thread's row of shared memory so that the products can update the
+// thread's row of shared memory so that the product can update the
 // registers in place (the kernel's register budget has room for one
 // vector of hi and lo words, not two).
 template<int V, class CF>
 __device__ __forceinline__ void cvr_update_df_row(
     float* row, float (&uh)[V], float (&ul)[V], float e, float& pout, const CF& cf)
 {
-    auto half_step = [&](bool last, float& pp) {
-        static_for<0, V>([&](auto J) {
-            constexpr int j = decltype(J)::value;
-            row[j] = uh[j];
-        });
-        static_for<0, V>([&](auto I) {
-            constexpr int i = decltype(I)::value;
-            float s = cf.k(i), sl = 0.0f;
-            for (int j = 0; j < V; j++) {
-                const float x = row[j];
-                s = fmaf(cf.Bd(i, j), x, s);
-                sl = fmaf(cf.Bdl(i, j), x, sl);
-            }
-            df_acc(uh[i], ul[i], s, sl);
-            if (last) {
-                df_renorm(uh[i], ul[i]);
-                pp = fmaf(cf.g(i), uh[i], fmaf(cf.g(i), ul[i], pp));
-            }
-        });
-    };
-    float pp = cf.p0();
-    half_step(false, pp);
-    static_for<0, V / 2>([&](auto KI) {
-        constexpr int k = decltype(KI)::value;
-        float sn, s2;
-        rot_coeffs<float>(cf.th(k) * e, sn, s2);
-        const float a = uh[2 * k], b = uh[2 * k + 1];
-        const float da = -fmaf(s2, a, sn * b);
-        const float db = fmaf(sn, a, -s2 * b);
-        df_acc(uh[2 * k], ul[2 * k], da, 0.0f);
-        df_acc(uh[2 * k + 1], ul[2 * k + 1], db, 0.0f);
+    rotate_df<V>(uh, ul, e, cf);
+    static_for<0, V>([&](auto J) {
+        constexpr int j = decltype(J)::value;
+        row[j] = uh[j];
     });
-    half_step(true, pp);
+    float pp = cf.p0();
+    static_for<0, V>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        float s = cf.k(i), sl = 0.0f;
+        for (int j = 0; j < V; j++) {
+            const float x = row[j];
+            s = fmaf(cf.Bd(i, j), x, s);
+            sl = fmaf(cf.Bdl(i, j), x, sl);
+        }
+        df_acc(uh[i], ul[i], s, sl);
+        df_renorm(uh[i], ul[i]);
+        pp = fmaf(cf.g(i), uh[i], fmaf(cf.g(i), ul[i], pp));
+    });
     pout = pp;
 }
 

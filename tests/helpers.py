@@ -66,25 +66,30 @@ def golden_cases():
 
 
 def plane_basis_step(c, L, d, e):
-    """One update of the engine's plane-basis form (numpy, FP64) from a
+    """One step of the engine's plane-basis form (numpy, FP64) from a
     constant block `c` with layout `L`: returns (d', P) for coherence
-    vector d and field e."""
+    vector d and field e. The kernels keep v = u + (Bh u + kh), u = Q^T d
+    (half a step ahead), rotate it and apply the full step Bd, k; d' comes
+    back through u' = (I + Bh)^-1 (v' - kh)."""
     import math
     V = L["V"]
     Q = c[L["Q"]:L["Q"] + V * V].reshape(V, V)
+    Bh = c[L["Bh"]:L["Bh"] + V * V].reshape(V, V)
+    kh = c[L["kh"]:L["kh"] + V]
     Bd = c[L["Bd"]:L["Bd"] + V * V].reshape(V, V)
     k_ = c[L["k"]:L["k"] + V]
     g = c[L["g"]:L["g"] + V]
     th = c[L["thdt"]:L["thdt"] + V // 2]
     u = Q.T @ d
-    w = u + (Bd @ u + k_)
+    v = u + (Bh @ u + kh)
     for k in range(V // 2):
         phi = th[k] * e
-        a, b = w[2 * k], w[2 * k + 1]
-        w[2 * k] = math.cos(phi) * a - math.sin(phi) * b
-        w[2 * k + 1] = math.sin(phi) * a + math.cos(phi) * b
-    u2 = w + (Bd @ w + k_)
-    return Q @ u2, c[L["p0"]] + g @ u2
+        a, b = v[2 * k], v[2 * k + 1]
+        v[2 * k] = math.cos(phi) * a - math.sin(phi) * b
+        v[2 * k + 1] = math.sin(phi) * a + math.cos(phi) * b
+    v2 = v + (Bd @ v + k_)
+    u2 = np.linalg.solve(np.eye(V) + Bh, v2 - kh)
+    return Q @ u2, c[L["p0"]] + g @ v2
 
 
 def tuning(C_=0, NT=0, depth=0, graph=0):

@@ -59,11 +59,33 @@ def test_plane_basis_step_equals_dense_rodrigues(native, N, seed):
     Bd = c[L["Bd"]:L["Bd"] + V * V]
     Bdl = c[L["Bdl"]:L["Bdl"] + V * V]
     np.testing.assert_array_equal(Bd - Bd.astype(np.float32).astype(np.float64), Bdl)
-    # observables: inversion is d[N(N-1)]
+    # the full step the kernels apply is two half steps: I + Bd = (I + Bh)^2
+    # and k = (I + Bh) kh + kh
+    Bh = c[L["Bh"]:L["Bh"] + V * V].reshape(V, V)
+    kh = c[L["kh"]:L["kh"] + V]
+    A = np.eye(V) + Bh
+    np.testing.assert_allclose(Bd.reshape(V, V), A @ A - np.eye(V), rtol=0,
+                               atol=1e-14)
+    np.testing.assert_allclose(c[L["k"]:L["k"] + V], A @ kh + kh, rtol=0,
+                               atol=1e-14 * max(1.0, np.abs(kh).max()))
+    # observables act on the kernels' state v = (I + Bh) u + kh: inversion
+    # is d[N(N-1)], populations are the reference's rho_mm
     d = rng.normal(size=V)
     u = Q.T @ d
-    inv = c[L["inv"]:L["inv"] + V] @ u + c[L["inv_c"]]
+    v = A @ u + kh
+    inv = c[L["inv"]:L["inv"] + V] @ v + c[L["inv_c"]]
     assert abs(inv - d[N * (N - 1)]) < 1e-12
+    pops = np.array([c[L["pop"] + m * V:L["pop"] + (m + 1) * V] @ v
+                     + c[L["pop_c"] + m] for m in range(N)])
+    assert abs(pops.sum() - 1.0) < 1e-12
+    # the initial state is v0 = (I + Bh) u0 + kh with u0 = Q^T d0, and d0
+    # gives the initial populations of the scenario's density matrix
+    v0 = c[L["u0"]:L["u0"] + V]
+    u0 = np.linalg.solve(A, v0 - kh)
+    pop0 = np.array([c[L["pop"] + m * V:L["pop"] + (m + 1) * V] @ v0
+                     + c[L["pop_c"] + m] for m in range(N)])
+    np.testing.assert_allclose(pop0.sum(), 1.0, atol=1e-12)
+    assert np.isfinite(u0).all()
 
 
 def test_cayley_constants(native):
