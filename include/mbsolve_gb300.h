@@ -106,12 +106,28 @@ typedef struct mbg_region {
     double x_end;
 } mbg_region;
 
+/* field boundary conditions (bc_field, device.hpp:38-79) */
+#define MBG_BC_PMC 0    /* H = 0 beyond both ends: what every reference
+                           solver applies (bc_field_reflectivity is stored,
+                           and ignored, solver_cpu_fdtd.tpp:263-275) */
+#define MBG_BC_MIRROR 1 /* no reference counterpart: semi-transparent
+                           mirrors of power reflectivity refl_left and
+                           refl_right at the ends. The H value beyond each
+                           end is tied to the end point's E as an impedance
+                           wall: H = +k E (left), H = -k E (right) with
+                           k Z = (1 - r)/(1 + r), r = sqrt(refl), Z the wave
+                           impedance of the end point's material. refl = 1
+                           is the PMC boundary, refl = 0 absorbs. */
+
 /* device (device.hpp:152-216) */
 typedef struct mbg_device {
     uint32_t num_materials;
     const mbg_material* materials;
     uint32_t num_regions;
     const mbg_region* regions;
+    int32_t bc_kind;    /* MBG_BC_*; 0 (PMC) reproduces the reference */
+    double refl_left;   /* MBG_BC_MIRROR: power reflectivities in [0, 1] */
+    double refl_right;
 } mbg_device;
 
 /* source (source.hpp:35-261).  SECH: A*sech(beta t - phase)*sin(2 pi f t -

@@ -15,6 +15,7 @@ MBG_SHAPE_TABLE, MBG_SHAPE_SECH, MBG_SHAPE_GAUSSIAN = 0, 1, 2
  MBG_RECORD_DENSITY, MBG_RECORD_INVERSION) = range(5)
 MBG_RELAX_NONE, MBG_RELAX_LINDBLAD = 0, 1
 MBG_FIELD_IC_CONST, MBG_FIELD_IC_VALUES = 0, 1
+MBG_BC_PMC, MBG_BC_MIRROR = 0, 1
 
 PD = C.POINTER(C.c_double)
 
@@ -57,6 +58,9 @@ class mbg_device(C.Structure):
         ("materials", C.POINTER(mbg_material)),
         ("num_regions", C.c_uint32),
         ("regions", C.POINTER(mbg_region)),
+        ("bc_kind", C.c_int32),
+        ("refl_left", C.c_double),
+        ("refl_right", C.c_double),
     ]
 
 

@@ -44,6 +44,9 @@ struct run_desc {
     double dx_inv;
     uint32_t src_begin, src_end;
     uint32_t rec_begin, rec_end;
+    // mirror boundary (MBG_BC_MIRROR): H beyond the left end = k_left E[0],
+    // beyond the right end = -k_right E[n_x - 1]; 0 for PMC (H = 0)
+    double k_left, k_right;
 };
 
 // A source after set-up (solver_cpu_fdtd.tpp:185-202): grid index and an

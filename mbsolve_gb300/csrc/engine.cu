@@ -201,6 +201,33 @@ run_setup setup_run(const solver_kind& k, const mbg_device* dev, const mbg_scena
     for (uint32_t i = 0; i < dev->num_regions; i++)
         r.regions.push_back({ dev->regions[i].material, dev->regions[i].x_start,
                               dev->regions[i].x_end });
+    // field boundary: the reference applies H = 0 beyond both ends whatever
+    // bc_field it is given (solver_cpu_fdtd.tpp:263-275); MBG_BC_MIRROR ties
+    // H beyond each end to the end point's E (impedance wall of reflection
+    // coefficient r = sqrt(refl) for E)
+    if (dev->bc_kind == MBG_BC_MIRROR) {
+        if (!(dev->refl_left >= 0.0 && dev->refl_left <= 1.0 && dev->refl_right >= 0.0 &&
+              dev->refl_right <= 1.0))
+            throw invalid_argument("mirror reflectivity must lie in [0, 1]");
+        auto wall = [&](double x, double refl) {
+            // material of the end point: the first region containing it
+            // (solver_cpu_fdtd.tpp:119-125)
+            const mbg_material* mt = nullptr;
+            for (uint32_t i = 0; i < dev->num_regions && !mt; i++)
+                if (x >= dev->regions[i].x_start && x <= dev->regions[i].x_end)
+                    mt = &dev->materials[dev->regions[i].material];
+            if (!mt) throw invalid_argument("region not found");
+            const double z = std::sqrt(MU0 * mt->rel_permeability / (EPS0 * mt->rel_permittivity));
+            const double rr = std::sqrt(refl);
+            return (1.0 - rr) / ((1.0 + rr) * z);
+        };
+        if (r.n_x > 1) {
+            r.k_left = wall(0.0, dev->refl_left);
+            r.k_right = wall((r.n_x - 1) * r.dx, dev->refl_right);
+        }
+    } else if (dev->bc_kind != MBG_BC_PMC) {
+        throw invalid_argument("unknown field boundary condition");
+    }
     // initial fields
     r.e_kind = sc->e_init_kind;
     r.e_val = sc->e_init_value;
@@ -967,6 +994,8 @@ private:
             rd.n_x = rs.n_x;
             rd.n_t = rs.n_t;
             rd.dx_inv = 1.0 / rs.dx;
+            rd.k_left = rs.k_left;
+            rd.k_right = rs.k_right;
             rd.src_begin = (uint32_t) srcs.size();
             for (const auto& s : rs.sources) {
                 if (!s.on_grid) continue;  // outside the grid: never applied

@@ -47,6 +47,9 @@ struct run_setup {
         double x0, x1;
     };
     std::vector<region_s> regions;
+    // MBG_BC_MIRROR: H beyond the left end = k_left E[0], beyond the right
+    // end = -k_right E[n_x - 1]; both 0 for the PMC boundary
+    double k_left = 0, k_right = 0;
     int e_kind = 0, h_kind = 0;
     double e_val = 0, h_val = 0;
     std::vector<double> e_vals, h_vals;

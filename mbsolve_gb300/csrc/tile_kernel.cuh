@@ -81,6 +81,11 @@ __device__ __forceinline__ bool tile_steps(
     const creg_t creg(sh_coef);
     const int nsrc = tl.overflow ? (int) (rd.src_end - rd.src_begin) : tl.nsrc;
     const int nrec = tl.overflow ? (int) (rd.rec_end - rd.rec_begin) : tl.nrec;
+    // mirror boundary: this thread holds the run's last point (index jr),
+    // whose E update reads H beyond the end = -k_right E
+    const int64_t jr = nx - 1 - l0;
+    const bool edge_r = rd.k_right != 0.0 && jr >= 0 && jr < C;
+    const T k_right = (T) rd.k_right, k_left = (T) rd.k_left;
 
     for (int m = 0; m < nsteps; m++) {
         const uint64_t n = step0 + (uint64_t) m;
@@ -95,6 +100,21 @@ __device__ __forceinline__ bool tile_steps(
         if (lane == 31) {
             hr = (warp + 1 < NW) ? sh_a[warp + 1] : T(0);
             if constexpr (DF) hrl = (warp + 1 < NW) ? sh_al[warp + 1] : T(0);
+        }
+        if (edge_r) {
+            // the point beyond the end holds zero state and is never
+            // updated or stored: its H register (or hr) carries the wall
+#pragma unroll
+            for (int j = 0; j < C; j++) {
+                if (j != jr) continue;
+                if (j + 1 < C) {
+                    H[j + 1] = -k_right * E[j];
+                    if constexpr (DF) Hl[j + 1] = -k_right * El[j];
+                } else {
+                    hr = -k_right * E[j];
+                    if constexpr (DF) hrl = -k_right * El[j];
+                }
+            }
         }
 #pragma unroll
         for (int j = 0; j < C; j++) {
@@ -156,8 +176,9 @@ __device__ __forceinline__ bool tile_steps(
                     H[j] += block(j)[pre::FD_C] * (E[j] - ep);
                 }
             } else if (l == 0) {
-                H[j] = T(0);
-                if constexpr (DF) Hl[j] = T(0);
+                // PMC: H = 0 (solver_cpu_fdtd.tpp:273); mirror: k_left E
+                H[j] = k_left != T(0) ? k_left * E[j] : T(0);
+                if constexpr (DF) Hl[j] = k_left != T(0) ? k_left * El[j] : T(0);
             }
         }
         // ---- density matrix and polarisation current at every point
@@ -258,6 +279,16 @@ __device__ __forceinline__ bool tile_steps(
                     }
                 }
             }
+        }
+    }
+    if (edge_r) {
+        // the point beyond the end goes back to zero state (a bulk store
+        // rounded up to 16 bytes may write it into the run's padding)
+#pragma unroll
+        for (int j = 0; j + 1 < C; j++) {
+            if (j != jr) continue;
+            H[j + 1] = T(0);
+            if constexpr (DF) Hl[j + 1] = T(0);
         }
     }
     return true;

@@ -234,6 +234,18 @@ class bc_field_reflectivity(bc_field):
         return self._r
 
 
+class bc_field_mirror(bc_field_reflectivity):
+    """Not in the reference: semi-transparent mirrors of power reflectivity
+    refl_left and refl_right at the device ends, applied by the gpu-fdtd
+    solvers (MBG_BC_MIRROR: H beyond each end tied to the end point's E as
+    an impedance wall with E-field reflection coefficient sqrt(refl);
+    1 is the reference's PMC boundary, 0 absorbs). The reference's own
+    bc_field_reflectivity stays stored and unapplied, as in its solvers."""
+
+    def __init__(self, refl_left=1.0, refl_right=1.0):
+        bc_field_reflectivity.__init__(self, refl_left, refl_right)
+
+
 class region:
     """device.hpp:82-150."""
 
@@ -752,6 +764,14 @@ def to_pod(dev, scen, bundle=None):
     d.materials = mats
     d.num_regions = len(regs)
     d.regions = rarr
+    bc = dev.get_bc_field()
+    if isinstance(bc, bc_field_mirror):
+        d.bc_kind = T.MBG_BC_MIRROR
+        d.refl_left = bc.get_refl_left()
+        d.refl_right = bc.get_refl_right()
+    else:
+        d.bc_kind = T.MBG_BC_PMC
+        d.refl_left = d.refl_right = 1.0
     b.device = b.hold(d)
 
     s = T.mbg_scenario()

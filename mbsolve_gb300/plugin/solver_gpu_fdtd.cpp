@@ -119,6 +119,11 @@ void describe(
     d.dev.materials = d.mats.data();
     d.dev.num_regions = (uint32_t) d.regions.size();
     d.dev.regions = d.regions.data();
+    /* the reference's solvers apply H = 0 beyond both ends whatever
+     * bc_field the device holds (solver_cpu_fdtd.tpp:263-275) */
+    d.dev.bc_kind = MBG_BC_PMC;
+    d.dev.refl_left = 1.0;
+    d.dev.refl_right = 1.0;
 
     mbg_scenario& s = d.scen;
     std::memset(&s, 0, sizeof(s));

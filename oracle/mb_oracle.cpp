@@ -943,6 +943,10 @@ struct solver {
     };
     std::vector<src> sources;
     uint64_t steps_done = 0;
+    /* MBG_BC_MIRROR (no reference counterpart): H beyond the left end is
+     * wall_l * E[0], beyond the right end -wall_r * E[n_x - 1]; 0 is the
+     * reference's PMC boundary */
+    real wall_l = 0, wall_r = 0;
 };
 
 /* common_fdtd.hpp:52-123 */
@@ -1005,6 +1009,26 @@ static solver* create(
     s->endtime = sc->endtime;
     s->dx_inv = 1.0 / s->dx;
     uint32_t n = s->n_x;
+
+    /* mirror walls: an impedance wall H = E / Z_w with
+     * (Z_w - Z) / (Z_w + Z) = sqrt(refl), Z of the end point's material */
+    if (dev->bc_kind == MBG_BC_MIRROR && n > 1) {
+        auto wall = [&](real x, real refl) -> real {
+            for (uint32_t r = 0; r < dev->num_regions; r++) {
+                const mbg_region& rg = dev->regions[r];
+                if (x >= rg.x_start && x <= rg.x_end) {
+                    const mbg_material& mt = dev->materials[rg.material];
+                    real z = std::sqrt(MU0 * mt.rel_permeability /
+                                       (EPS0 * mt.rel_permittivity));
+                    real zw = z * (1.0 + std::sqrt(refl)) / (1.0 - std::sqrt(refl));
+                    return 1.0 / zw; /* 0 for refl = 1 */
+                }
+            }
+            throw std::invalid_argument("region not found");
+        };
+        s->wall_l = wall(0.0, dev->refl_left);
+        s->wall_r = wall((n - 1) * s->dx, dev->refl_right);
+    }
 
     /* per-material constants (tpp:76-89): FDTD and Lindblad */
     struct fd {
@@ -1234,8 +1258,8 @@ static void run(solver* s, int threads, uint32_t max_steps)
             for (int64_t i = 1; i < n; i++) H[i] += fc[i] * (E[i] - E[i - 1]);
 #pragma omp single
             {
-                H[0] = 0;
-                H[n] = 0;
+                H[0] = s->wall_l != 0 ? s->wall_l * E[0] : 0;
+                H[n] = s->wall_r != 0 ? -s->wall_r * E[n - 1] : 0;
             }
             if (s->algo == ALGO_RODR) {
 #pragma omp for schedule(static)
