@@ -154,6 +154,10 @@ typedef struct mbg_record {
     double interval;
     double position;
     int32_t is_complex;
+    int32_t coherence; /* density records with row != col: 0 records zero,
+                          as every reference solver (solver_cpu_fdtd.tpp:
+                          314-318); 1 records rho[row][col] (real and
+                          imaginary part; no reference counterpart) */
 } mbg_record;
 
 /* scenario (scenario.hpp:164-335) with constant density initial condition

@@ -87,6 +87,7 @@ class mbg_record(C.Structure):
         ("interval", C.c_double),
         ("position", C.c_double),
         ("is_complex", C.c_int32),
+        ("coherence", C.c_int32),
     ]
 
 

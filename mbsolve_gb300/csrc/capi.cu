@@ -442,7 +442,7 @@ size_t mbg_material_layout(const char* algo, uint32_t N, char* buf, size_t len)
           << "\nu0=" << L.z0 << "\nbdx=" << mbg::pre::FD_BDX << "\nbdx_lo=" << mbg::pre::FD_BDX_LO
           << "\ncH_lo=" << mbg::pre::FD_C_LO << "\nbG=" << mbg::pre::FD_G
           << "\ninv=" << L.inv << "\ninv_c=" << L.inv_c << "\npop=" << L.pop << "\npop_c=" << L.pop_c
-          << "\nQ=" << L.Q << "\nBh=" << L.Bh << "\nkh=" << L.kh << "\nstage=" << L.stage << "\nstride=" << L.stride;
+          << "\nQ=" << L.Q << "\nBh=" << L.Bh << "\nkh=" << L.kh << "\ncoh=" << L.coh << "\ncoh_c=" << L.coh_c << "\nstage=" << L.stage << "\nstride=" << L.stride;
     } else if (a == "reg-cayley") {
         mbg::pre::cay_layout L = mbg::pre::make_cay_layout((int) N);
         s << "a=" << L.a << "\nb=" << L.b << "\ncH=" << L.cH << "\ngamma=" << L.gam << "\nhas_qm=" << L.has_qm

@@ -66,6 +66,9 @@ struct rec_desc {
     uint64_t rows;
     double ratio;        // interval ratio dt/interval (1 when every step)
     uint64_t offset;     // into the scratch of the run's records
+    int32_t coh;         // 1: density record of rho[row][col], row != col,
+                         // real part at offset, imaginary part rows * cols
+                         // later (the reference records zero)
 };
 
 // copy_list_entry_dev::hasto_record (copy_list_entry.hpp:269-275). The

@@ -251,6 +251,12 @@ run_setup setup_run(const solver_kind& k, const mbg_device* dev, const mbg_scena
         d.type = rc.type;
         d.row_idx = rc.row;
         d.col_idx = rc.col;
+        // coherence records (no reference counterpart) need a density
+        // matrix entry that exists; otherwise they stay zero like the
+        // reference's
+        d.coh = (rc.coherence && rc.type == MBG_RECORD_DENSITY && rc.row != rc.col &&
+                 rc.is_complex && k.algo != ALGO_NOOP && (int) rc.row < k.N && (int) rc.col < k.N)
+            ? 1 : 0;
         if (rc.interval <= r.dt) {
             d.rows = r.n_t;
             d.ratio = 1.0;

@@ -496,6 +496,31 @@ __device__ __forceinline__ T cvr_record_value(
     return T(0);
 }
 
+// Real (im false) or imaginary part of rho[row][col] (row != col) of a
+// coherence record at one point (no reference counterpart: the reference
+// records zero, solver_cpu_fdtd.tpp:314-318): rows of the material block
+// on the kernels' state (coh, coh_c in cvr_layout).
+template<typename T, int V>
+__device__ __forceinline__ T cvr_coherence_value(
+    const rec_desc& rc,
+    const T (&z)[V > 0 ? V : 1],
+    const T* mcb,
+    int N,
+    bool im)
+{
+    if constexpr (V == 0) {
+        return T(0);
+    } else {
+        pre::cvr_layout L = pre::make_cvr_layout(N);
+        const int a = (int) min(rc.row_idx, rc.col_idx), b = (int) max(rc.row_idx, rc.col_idx);
+        const int r = 2 * (b * (b - 1) / 2 + a) + (im ? 1 : 0);
+        T s = mcb[L.coh_c + r];
+#pragma unroll
+        for (int k = 0; k < V; k++) s += mcb[L.coh + r * V + k] * z[k];
+        return (im && rc.row_idx > rc.col_idx) ? -s : s;
+    }
+}
+
 template<typename T>
 __device__ __forceinline__ void store_record(
     const kparams<T>& p,

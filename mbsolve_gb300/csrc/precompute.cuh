@@ -122,6 +122,9 @@ struct cvr_layout {
     int Bd, Bdl, k, g, thdt, z0, inv, inv_c, pop, pop_c;
     int Q;       // the plane basis (inspection only; kernels stop before it)
     int Bh, kh;  // the half step (inspection only)
+    // coherence records: rho[j][k] (j < k, pair q = k(k-1)/2 + j) is
+    // coh[(2q) V ..] . v + coh_c[2q] + i (coh[(2q+1) V ..] . v + coh_c[2q+1])
+    int coh, coh_c;
     int stage;   // leading part a kernel stages in shared memory
     int stride;
 };
@@ -167,6 +170,11 @@ MBG_HD cvr_layout make_cvr_layout(int N)
     o += L.V * L.V;
     L.kh = o;
     o += L.V;
+    const int P = N * (N - 1) / 2;
+    L.coh = o;
+    o += 2 * P * L.V;
+    L.coh_c = o;
+    o += 2 * P;
     L.stride = (o + 3) & ~3;
     return L;
 }
@@ -905,6 +913,29 @@ MBG_HD int cvr_precompute(const mat_in& m, int Nsolver, double* ws, double* out)
         out[L.pop_c + mm] = population_const(N, mm);
         compose(out + L.pop + mm * V, out[L.pop_c + mm]);
     }
+    // coherences: rho = I/N + 1/2 sum_i d_i g_i, so rho[j][k] (j != k) is
+    // 1/2 sum_i (g_i)[j][k] d_i: real and imaginary rows on d, then on u
+    // (d = Q u), then composed with A1^-1 like the other records
+    for (int kk = 1; kk < N; kk++)
+        for (int jj = 0; jj < kk; jj++) {
+            const int q = kk * (kk - 1) / 2 + jj;
+            for (int part = 0; part < 2; part++) {
+                for (int i = 0; i < V; i++) t2[i] = 0.0;
+                for (int i = 0; i < V; i++) {
+                    int nz = generator_entries(N, i, gr, gc, gv);
+                    for (int e = 0; e < nz; e++)
+                        if (gr[e] == jj && gc[e] == kk) t2[i] += 0.5 * (part == 0 ? gv[e].re : gv[e].im);
+                }
+                double* row = out + L.coh + (2 * q + part) * V;
+                for (int c = 0; c < V; c++) {
+                    double s = 0.0;
+                    for (int i = 0; i < V; i++) s += t2[i] * Q[i * V + c];
+                    row[c] = s;
+                }
+                out[L.coh_c + 2 * q + part] = 0.0;
+                compose(row, out[L.coh_c + 2 * q + part]);
+            }
+        }
     return 0;
 }
 

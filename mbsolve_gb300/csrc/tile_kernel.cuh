@@ -249,7 +249,7 @@ __device__ __forceinline__ bool tile_steps(
                     if (l < lo || l >= hi) continue;
                     const T ev = DF ? E[j] + El[j] : E[j];
                     const T hv = DF ? H[j] + Hl[j] : H[j];
-                    T v = T(0);
+                    T v = T(0), vi = T(0);
                     if constexpr (ALGO == 2) {
                         switch (rc.type) {
                         case 0: v = ev; break;
@@ -261,6 +261,19 @@ __device__ __forceinline__ bool tile_steps(
 #pragma unroll
                             for (int q = 0; q < LEV; q++)
                                 if (rc.row_idx == rc.col_idx && rc.row_idx == (uint32_t) q) v = R[j][q];
+                            if (rc.coh) {
+                                // packed upper triangle: (re, im) of rho[a][b], a < b
+                                const uint32_t a = min(rc.row_idx, rc.col_idx);
+                                const uint32_t b = max(rc.row_idx, rc.col_idx);
+                                const uint32_t qq = b * (b - 1) / 2 + a;
+#pragma unroll
+                                for (int q = 0; q < LEV * (LEV - 1) / 2; q++)
+                                    if (qq == (uint32_t) q) {
+                                        v = R[j][LEV + 2 * q];
+                                        vi = R[j][LEV + 2 * q + 1];
+                                    }
+                                if (rc.row_idx > rc.col_idx) vi = -vi;
+                            }
                             break;
                         }
                     } else {
@@ -270,12 +283,25 @@ __device__ __forceinline__ bool tile_steps(
                         for (int q = 0; q < DDv; q++) u[q] = DF ? R[j][q] + Rl[j][q] : R[j][q];
                         // the padded shared copy lacks the record rows
                         const T* rb = PADC ? p.mc + (uint64_t) M[j] * p.mstride : block(j);
-                        v = cvr_record_value<T, D>(rc, ev, hv, P[j], u, rb, LEV);
+                        if (rc.coh) {
+                            // the coherence rows lie after the part a tile
+                            // stages in shared memory: global block
+                            const T* gb = p.mc + (uint64_t) M[j] * p.mstride;
+                            v = cvr_coherence_value<T, D>(rc, u, gb, LEV, false);
+                            vi = cvr_coherence_value<T, D>(rc, u, gb, LEV, true);
+                        } else {
+                            v = cvr_record_value<T, D>(rc, ev, hv, P[j], u, rb, LEV);
+                        }
                     }
                     const uint64_t row = rc.ratio == 1.0 ? n : (uint64_t) floor(rc.ratio * (double) n);
                     if (row < rc.rows) {
-                        p.scratch[rc.offset + row * rc.cols + (uint64_t) (l - rc.pos)] = v;
+                        const uint64_t at = rc.offset + row * rc.cols + (uint64_t) (l - rc.pos);
+                        p.scratch[at] = v;
                         if (!isfinite(v)) atomicOr(p.status, STATUS_NONFINITE);
+                        if (rc.coh) {
+                            p.scratch[at + rc.rows * rc.cols] = vi;
+                            if (!isfinite(vi)) atomicOr(p.status, STATUS_NONFINITE);
+                        }
                     }
                 }
             }

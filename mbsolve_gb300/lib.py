@@ -509,6 +509,19 @@ class record:
         return self._complex
 
 
+class coherence_record(record):
+    """Not in the reference: a density record of an off-diagonal entry
+    rho[row][col] (one-based indices, row != col) that records its value,
+    real and imaginary part. The reference's record of the same entry stays
+    zero (solver_cpu_fdtd.tpp:314-318), and so does this package's."""
+
+    def __init__(self, name, row_idx, col_idx, interval=0.0, position=-1.0):
+        if int(row_idx) == int(col_idx):
+            raise RuntimeError("coherence record needs row != col")
+        record.__init__(self, name, record.density, row_idx, col_idx,
+                        interval, position)
+
+
 class result:
     """result.hpp:37-120: row-major [rows x cols] real and imaginary data."""
 
@@ -840,6 +853,7 @@ def to_pod(dev, scen, bundle=None):
         rarr2[i].interval = r.get_interval()
         rarr2[i].position = r.get_position()
         rarr2[i].is_complex = int(r.is_complex())
+        rarr2[i].coherence = int(isinstance(r, coherence_record))
     s.num_records = len(recs)
     s.records = rarr2
     b.scenario = b.hold(s)

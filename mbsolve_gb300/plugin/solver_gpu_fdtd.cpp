@@ -147,6 +147,7 @@ void describe(
         r.interval = rec->get_interval();
         r.position = rec->get_position();
         r.is_complex = rec->is_complex() ? 1 : 0;
+        r.coherence = 0; /* off-diagonal entries stay zero, as the reference */
         d.records.push_back(r);
     }
     s.num_records = (uint32_t) d.records.size();

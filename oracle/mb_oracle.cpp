@@ -621,6 +621,21 @@ static std::vector<real> coherence_vector(
 }
 
 /* populations from a coherence vector (cvr.hpp:289-336) */
+/* rho[row][col] (row != col) from the coherence vector: rho = I/N +
+ * 1/2 sum_i d_i g_i with the generators of cvr.hpp:52-93 (u_jk: 1 at (j, k)
+ * and (k, j); v_jk: -i at (j, k), +i at (k, j); pairs j < k in the order
+ * k = 1..N-1, j = 0..k-1), so rho[j][k] = (d_u - i d_v) / 2 and
+ * rho[k][j] its conjugate. No reference counterpart: the reference leaves
+ * coherence records zero (solver_cpu_fdtd.tpp:314-318). */
+static cplx cvr_coherence(int N, const real* d, unsigned int row, unsigned int col)
+{
+    unsigned int j = row < col ? row : col, k = row < col ? col : row;
+    int P = N * (N - 1) / 2;
+    int q = (int) (k * (k - 1) / 2 + j);
+    cplx r(0.5 * d[q], -0.5 * d[P + q]);
+    return row < col ? r : std::conj(r);
+}
+
 static real cvr_population(int N, const real* d, unsigned int m)
 {
     if (N == 2) {
@@ -904,6 +919,8 @@ struct record_plan {
     int type = 0;
     uint32_t row_idx = 0, col_idx = 0;
     bool is_complex = false;
+    bool coherence = false; /* record rho[row][col] (no reference
+                               counterpart; the reference records zero) */
 
     bool hasto_record(uint64_t iteration) const
     {
@@ -1158,6 +1175,8 @@ static solver* create(
         rp.is_complex = rec.is_complex != 0;
         rp.row_idx = rec.row;
         rp.col_idx = rec.col;
+        rp.coherence = rec.coherence != 0 && rec.row != rec.col &&
+            rec.type == MBG_RECORD_DENSITY;
         rp.offset_real = scratch_size;
         rp.offset_imag = scratch_size + rp.cols * rp.rows;
         scratch_size += rp.cols * rp.rows;
@@ -1197,8 +1216,18 @@ static solver* create(
     return s.release();
 }
 
+/* rho[row][col] of a coherence record at point i (see cvr_coherence) */
+static cplx coherence_value(const solver* s, const record_plan& rp, uint64_t i)
+{
+    if (s->algo == ALGO_RODR)
+        return cvr_coherence(s->N, &s->d_cvr[i * s->V], rp.row_idx, rp.col_idx);
+    if (s->algo == ALGO_CAYLEY) return s->d_cay[i](rp.row_idx, rp.col_idx);
+    return cplx(0.0, 0.0);
+}
+
 static real record_value(const solver* s, const record_plan& rp, uint64_t i)
 {
+    if (rp.coherence) return coherence_value(s, rp, i).real();
     switch (rp.type) {
     case MBG_RECORD_ELECTRIC:
         return s->e[i];
@@ -1280,6 +1309,12 @@ static void run(solver* s, int threads, uint32_t max_steps)
 #pragma omp for schedule(static)
                 for (int64_t i = (int64_t) pos; i < (int64_t) (pos + cols); i++)
                     if (i < n) s->scratch[o_r + i - pos] = record_value(s, rp, i);
+                if (rp.coherence) {
+                    int64_t o_i = o_r - (int64_t) rp.offset_real + (int64_t) rp.offset_imag;
+#pragma omp for schedule(static)
+                    for (int64_t i = (int64_t) pos; i < (int64_t) (pos + cols); i++)
+                        if (i < n) s->scratch[o_i + i - pos] = coherence_value(s, rp, i).imag();
+                }
             }
         }
     }
