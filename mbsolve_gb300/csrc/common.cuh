@@ -66,10 +66,13 @@ struct rec_desc {
     uint64_t rows;
     double ratio;        // interval ratio dt/interval (1 when every step)
     uint64_t offset;     // into the scratch of the run's records
-    int32_t coh;         // 1: density record of rho[row][col], row != col,
-                         // real part at offset, imaginary part rows * cols
-                         // later (the reference records zero)
 };
+
+// Kernel-side record types beyond MBG_RECORD_*: a coherence record (the
+// entry rho[row][col], row != col; the reference records zero) becomes two
+// device records, its real and its imaginary part, each stored like a real
+// record (the imaginary part rows * cols after the real part).
+enum : int32_t { REC_COH_RE = 5, REC_COH_IM = 6 };
 
 // copy_list_entry_dev::hasto_record (copy_list_entry.hpp:269-275). The
 // reference evaluates floor(ratio*(0-1)) on an unsigned wrap-around at

@@ -254,9 +254,8 @@ run_setup setup_run(const solver_kind& k, const mbg_device* dev, const mbg_scena
         // coherence records (no reference counterpart) need a density
         // matrix entry that exists; otherwise they stay zero like the
         // reference's
-        d.coh = (rc.coherence && rc.type == MBG_RECORD_DENSITY && rc.row != rc.col &&
-                 rc.is_complex && k.algo != ALGO_NOOP && (int) rc.row < k.N && (int) rc.col < k.N)
-            ? 1 : 0;
+        rs.coherence = rc.coherence && rc.type == MBG_RECORD_DENSITY && rc.row != rc.col &&
+            rc.is_complex && k.algo != ALGO_NOOP && (int) rc.row < k.N && (int) rc.col < k.N;
         if (rc.interval <= r.dt) {
             d.rows = r.n_t;
             d.ratio = 1.0;
@@ -482,6 +481,11 @@ __global__ void tile_uniform_kernel(
     bool same = true;
     for (int64_t l = lo + lane; l < hi; l += 32)
         if (mat[rd.offset + l] != m0) same = false;
+    // a mirror wall in the window (point 0 or the point beyond the end):
+    // the tile takes the non-uniform path, which alone applies the walls
+    const int64_t w0 = (int64_t) td.out_start - halo, w1 = (int64_t) td.out_start + td.out_len + halo;
+    if ((rd.k_left != 0.0 && w0 <= 0 && 0 < w1) || (rd.k_right != 0.0 && w0 <= (int64_t) rd.n_x && (int64_t) rd.n_x < w1))
+        same = false;
     same = __all_sync(0xffffffffu, same);
     if (lane == 0) tiles[t].uniform_mat = same ? m0 : -1;
 }
@@ -1076,6 +1080,12 @@ private:
             for (const auto& rc : runs_[r].records) {
                 rec_desc d = rc.d;
                 d.offset += sbase;
+                if (rc.coherence) {
+                    d.type = REC_COH_RE;
+                    recs.push_back(d);
+                    d.type = REC_COH_IM;
+                    d.offset += d.rows * d.cols;
+                }
                 recs.push_back(d);
             }
             rd.rec_end = (uint32_t) recs.size();

@@ -64,6 +64,7 @@ struct run_setup {
     struct record_s {
         rec_desc d;  // offset relative to the run's first record
         bool is_complex;
+        bool coherence = false;  // rho[row][col], row != col (see REC_COH_RE)
     };
     std::vector<record_s> records;
     uint64_t scratch = 0;

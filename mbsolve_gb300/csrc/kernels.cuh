@@ -467,57 +467,40 @@ __device__ __forceinline__ T cvr_record_value(
         return pt;
     case 2:
         return h;
-    case 4: {  // inversion d[N(N-1)]
-        if (V == 0) return T(0);
-        pre::cvr_layout L = pre::make_cvr_layout(N);
-        T s = mcb[L.inv_c];
-#pragma unroll
-        for (int k = 0; k < (V > 0 ? V : 1); k++) s += mcb[L.inv + k] * z[k];
-        return s;
     }
-    case 3: {
-        if (V == 0) return T(0);
-        if (rc.row_idx != rc.col_idx) return T(0);  // coherences: left zero
-        pre::cvr_layout L = pre::make_cvr_layout(N);
-        int m = (int) rc.row_idx;
-        // out-of-range level: what cvr.hpp:289-336 returns for it
-        if (m >= N) {
-            if (N == 2)
-                m = 1;
-            else
-                return (N == 3) ? T(0) : T(1.0 / N);
-        }
-        T s = mcb[L.pop_c + m];
-#pragma unroll
-        for (int k = 0; k < (V > 0 ? V : 1); k++) s += mcb[L.pop + m * (V > 0 ? V : 1) + k] * z[k];
-        return s;
-    }
-    }
-    return T(0);
-}
-
-// Real (im false) or imaginary part of rho[row][col] (row != col) of a
-// coherence record at one point (no reference counterpart: the reference
-// records zero, solver_cpu_fdtd.tpp:314-318): rows of the material block
-// on the kernels' state (coh, coh_c in cvr_layout).
-template<typename T, int V>
-__device__ __forceinline__ T cvr_coherence_value(
-    const rec_desc& rc,
-    const T (&z)[V > 0 ? V : 1],
-    const T* mcb,
-    int N,
-    bool im)
-{
     if constexpr (V == 0) {
         return T(0);
     } else {
+        // inversion, population and coherence parts: one row of the
+        // material block on the state (inv, pop, coh in cvr_layout)
         pre::cvr_layout L = pre::make_cvr_layout(N);
-        const int a = (int) min(rc.row_idx, rc.col_idx), b = (int) max(rc.row_idx, rc.col_idx);
-        const int r = 2 * (b * (b - 1) / 2 + a) + (im ? 1 : 0);
-        T s = mcb[L.coh_c + r];
+        int row, c;
+        if (rc.type == 4) {  // inversion d[N(N-1)]
+            row = L.inv;
+            c = L.inv_c;
+        } else if (rc.type == 3) {
+            if (rc.row_idx != rc.col_idx) return T(0);  // coherences: left zero
+            int m = (int) rc.row_idx;
+            // out-of-range level: what cvr.hpp:289-336 returns for it
+            if (m >= N) {
+                if (N == 2)
+                    m = 1;
+                else
+                    return (N == 3) ? T(0) : T(1.0 / N);
+            }
+            row = L.pop + m * V;
+            c = L.pop_c + m;
+        } else {  // REC_COH_RE / REC_COH_IM: rho[a][b], a < b, pair q
+            const int a = (int) min(rc.row_idx, rc.col_idx), b = (int) max(rc.row_idx, rc.col_idx);
+            const int r = 2 * (b * (b - 1) / 2 + a) + (rc.type == REC_COH_IM ? 1 : 0);
+            row = L.coh + r * V;
+            c = L.coh_c + r;
+        }
+        T s = mcb[c];
 #pragma unroll
-        for (int k = 0; k < V; k++) s += mcb[L.coh + r * V + k] * z[k];
-        return (im && rc.row_idx > rc.col_idx) ? -s : s;
+        for (int k = 0; k < V; k++) s += mcb[row + k] * z[k];
+        // rho[b][a] is the conjugate of rho[a][b]
+        return (rc.type == REC_COH_IM && rc.row_idx > rc.col_idx) ? -s : s;
     }
 }
 

@@ -29,6 +29,7 @@ struct no_coef {
 
 struct tile_lists {
     int nsrc, nrec, overflow;
+    int wall;  // the window holds a mirror wall (run_desc k_left, k_right)
     src_desc src[TILE_MAX_SRC];
     rec_desc rec[TILE_MAX_REC];
 };
@@ -81,12 +82,34 @@ __device__ __forceinline__ bool tile_steps(
     const creg_t creg(sh_coef);
     const int nsrc = tl.overflow ? (int) (rd.src_end - rd.src_begin) : tl.nsrc;
     const int nrec = tl.overflow ? (int) (rd.rec_end - rd.rec_begin) : tl.nrec;
-    // mirror boundary: this thread holds the run's last point (index jr),
-    // whose E update reads H beyond the end = -k_right E
-    const int64_t jr = nx - 1 - l0;
-    const bool edge_r = rd.k_right != 0.0 && jr >= 0 && jr < C;
-    const T k_right = (T) rd.k_right, k_left = (T) rd.k_left;
-
+    // Mirror walls are handled only on tiles of the non-uniform path (the
+    // set-up marks a tile whose window holds a wall non-uniform): code that
+    // touches H around the time loop, even off its hot path, costs the
+    // uniform 2-level kernel 5-8 % (measured).
+    if (!UNIFORM && tl.wall && rd.k_right != 0.0) {
+        // mirror: the point beyond the right end loads as zero state; give
+        // it its wall value -k_right E[nx - 1] before the first step (the H
+        // update keeps it from then on). rd is the same in the whole CTA.
+        if (lane == 31) {
+            sh_b[warp] = E[C - 1];
+            if constexpr (DF) sh_bl[warp] = El[C - 1];
+        }
+        __syncthreads();
+        T el = __shfl_up_sync(0xffffffffu, E[C - 1], 1);
+        T ell = DF ? __shfl_up_sync(0xffffffffu, El[C - 1], 1) : T(0);
+        if (lane == 0) {
+            el = (warp > 0) ? sh_b[warp - 1] : T(0);
+            if constexpr (DF) ell = (warp > 0) ? sh_bl[warp - 1] : T(0);
+        }
+        const T k_right = (T) rd.k_right;
+#pragma unroll
+        for (int j = 0; j < C; j++)
+            if (l0 + j == nx) {
+                H[j] = -k_right * ((j > 0) ? E[j - 1] : el);
+                if constexpr (DF) Hl[j] = -k_right * ((j > 0) ? El[j - 1] : ell);
+            }
+        // sh_b is written again only after the next barrier (E phase)
+    }
     for (int m = 0; m < nsteps; m++) {
         const uint64_t n = step0 + (uint64_t) m;
         // ---- E: needs H (hi, lo) of the right neighbour
@@ -100,21 +123,6 @@ __device__ __forceinline__ bool tile_steps(
         if (lane == 31) {
             hr = (warp + 1 < NW) ? sh_a[warp + 1] : T(0);
             if constexpr (DF) hrl = (warp + 1 < NW) ? sh_al[warp + 1] : T(0);
-        }
-        if (edge_r) {
-            // the point beyond the end holds zero state and is never
-            // updated or stored: its H register (or hr) carries the wall
-#pragma unroll
-            for (int j = 0; j < C; j++) {
-                if (j != jr) continue;
-                if (j + 1 < C) {
-                    H[j + 1] = -k_right * E[j];
-                    if constexpr (DF) Hl[j + 1] = -k_right * El[j];
-                } else {
-                    hr = -k_right * E[j];
-                    if constexpr (DF) hrl = -k_right * El[j];
-                }
-            }
         }
 #pragma unroll
         for (int j = 0; j < C; j++) {
@@ -176,9 +184,31 @@ __device__ __forceinline__ bool tile_steps(
                     H[j] += block(j)[pre::FD_C] * (E[j] - ep);
                 }
             } else if (l == 0) {
-                // PMC: H = 0 (solver_cpu_fdtd.tpp:273); mirror: k_left E
-                H[j] = k_left != T(0) ? k_left * E[j] : T(0);
-                if constexpr (DF) Hl[j] = k_left != T(0) ? k_left * El[j] : T(0);
+                H[j] = T(0);  // PMC (solver_cpu_fdtd.tpp:273)
+                if constexpr (DF) Hl[j] = T(0);
+            }
+        }
+        if (!UNIFORM && tl.wall) {
+            // mirror walls (the thread holding point 0 or the point beyond
+            // the right end): H = k_left E[0] before the left end,
+            // -k_right E[nx - 1] beyond the right end (a point of zero
+            // state, never updated or stored), read by the end points' E
+            // updates in the next step. The flag lives in shared memory and
+            // the coefficients are read here: values held in registers
+            // across the time loop cost the 2-level kernel its register
+            // budget (coefficients reloaded every step).
+            const run_desc& rw = p.runs[p.tiles[blockIdx.x].run];
+            const T k_left = (T) rw.k_left, k_right = (T) rw.k_right;
+#pragma unroll
+            for (int j = 0; j < C; j++) {
+                const int64_t l = l0 + j;
+                if (l == 0 && k_left != T(0)) {
+                    H[j] = k_left * E[j];
+                    if constexpr (DF) Hl[j] = k_left * El[j];
+                } else if (l == nx && k_right != T(0)) {
+                    H[j] = -k_right * ((j > 0) ? E[j - 1] : el);
+                    if constexpr (DF) Hl[j] = -k_right * ((j > 0) ? El[j - 1] : ell);
+                }
             }
         }
         // ---- density matrix and polarisation current at every point
@@ -243,79 +273,64 @@ __device__ __forceinline__ bool tile_steps(
                 const int64_t lo = max((int64_t) rc.pos, (int64_t) td.out_start);
                 const int64_t hi = min((int64_t) rc.pos + rc.cols, (int64_t) td.out_start + td.out_len);
                 if (l0 + C <= lo || l0 >= hi) continue;
+                const uint64_t row = rc.ratio == 1.0 ? n : (uint64_t) floor(rc.ratio * (double) n);
+                if (row >= rc.rows) continue;
 #pragma unroll
                 for (int j = 0; j < C; j++) {
                     const int64_t l = l0 + j;
                     if (l < lo || l >= hi) continue;
                     const T ev = DF ? E[j] + El[j] : E[j];
                     const T hv = DF ? H[j] + Hl[j] : H[j];
-                    T v = T(0), vi = T(0);
+                    T v = T(0);
                     if constexpr (ALGO == 2) {
                         switch (rc.type) {
                         case 0: v = ev; break;
                         case 1: v = P[j]; break;
                         case 2: v = hv; break;
                         case 4: v = R[j][1] - R[j][0]; break;
-                        case 3:
-                            // constant indices keep R in registers
+                        default: {
+                            // populations (3) and coherence parts (REC_COH_*):
+                            // an entry of the packed matrix (diagonal, then
+                            // the upper triangle as (re, im) pairs); constant
+                            // indices keep R in registers
+                            const uint32_t a = min(rc.row_idx, rc.col_idx);
+                            const uint32_t b = max(rc.row_idx, rc.col_idx);
+                            uint32_t idx = rc.type == 3 ? (a == b ? a : 0xffffffffu)
+                                                        : LEV + 2 * (b * (b - 1) / 2 + a) +
+                                                            (rc.type == REC_COH_IM ? 1 : 0);
 #pragma unroll
-                            for (int q = 0; q < LEV; q++)
-                                if (rc.row_idx == rc.col_idx && rc.row_idx == (uint32_t) q) v = R[j][q];
-                            if (rc.coh) {
-                                // packed upper triangle: (re, im) of rho[a][b], a < b
-                                const uint32_t a = min(rc.row_idx, rc.col_idx);
-                                const uint32_t b = max(rc.row_idx, rc.col_idx);
-                                const uint32_t qq = b * (b - 1) / 2 + a;
-#pragma unroll
-                                for (int q = 0; q < LEV * (LEV - 1) / 2; q++)
-                                    if (qq == (uint32_t) q) {
-                                        v = R[j][LEV + 2 * q];
-                                        vi = R[j][LEV + 2 * q + 1];
-                                    }
-                                if (rc.row_idx > rc.col_idx) vi = -vi;
-                            }
+                            for (int q = 0; q < LEV * LEV; q++)
+                                if (idx == (uint32_t) q) v = R[j][q];
+                            if (rc.type == REC_COH_IM && rc.row_idx > rc.col_idx) v = -v;
                             break;
+                        }
                         }
                     } else {
                         constexpr int DDv = D > 0 ? D : 1;
                         T u[DDv];
 #pragma unroll
                         for (int q = 0; q < DDv; q++) u[q] = DF ? R[j][q] + Rl[j][q] : R[j][q];
-                        // the padded shared copy lacks the record rows
-                        const T* rb = PADC ? p.mc + (uint64_t) M[j] * p.mstride : block(j);
-                        if (rc.coh) {
-                            // the coherence rows lie after the part a tile
-                            // stages in shared memory: global block
-                            const T* gb = p.mc + (uint64_t) M[j] * p.mstride;
-                            v = cvr_coherence_value<T, D>(rc, u, gb, LEV, false);
-                            vi = cvr_coherence_value<T, D>(rc, u, gb, LEV, true);
-                        } else {
-                            v = cvr_record_value<T, D>(rc, ev, hv, P[j], u, rb, LEV);
-                        }
+                        // the padded shared copy lacks the record rows, the
+                        // staged copy the coherence rows
+                        const T* rb = (PADC || rc.type >= REC_COH_RE) ? p.mc + (uint64_t) M[j] * p.mstride
+                                                                       : block(j);
+                        v = cvr_record_value<T, D>(rc, ev, hv, P[j], u, rb, LEV);
                     }
-                    const uint64_t row = rc.ratio == 1.0 ? n : (uint64_t) floor(rc.ratio * (double) n);
-                    if (row < rc.rows) {
-                        const uint64_t at = rc.offset + row * rc.cols + (uint64_t) (l - rc.pos);
-                        p.scratch[at] = v;
-                        if (!isfinite(v)) atomicOr(p.status, STATUS_NONFINITE);
-                        if (rc.coh) {
-                            p.scratch[at + rc.rows * rc.cols] = vi;
-                            if (!isfinite(vi)) atomicOr(p.status, STATUS_NONFINITE);
-                        }
-                    }
+                    p.scratch[rc.offset + row * rc.cols + (uint64_t) (l - rc.pos)] = v;
+                    if (!isfinite(v)) atomicOr(p.status, STATUS_NONFINITE);
                 }
             }
         }
     }
-    if (edge_r) {
-        // the point beyond the end goes back to zero state (a bulk store
-        // rounded up to 16 bytes may write it into the run's padding)
+    if (!UNIFORM && tl.wall) {
+        // the point beyond the right end goes back to zero state (a bulk
+        // store rounded up to 16 bytes may write it into the run's padding)
 #pragma unroll
-        for (int j = 0; j + 1 < C; j++) {
-            if (j != jr) continue;
-            H[j + 1] = T(0);
-            if constexpr (DF) Hl[j + 1] = T(0);
-        }
+        for (int j = 0; j < C; j++)
+            if (l0 + j == nx) {
+                H[j] = T(0);
+                if constexpr (DF) Hl[j] = T(0);
+            }
     }
     return true;
 }
@@ -371,6 +386,10 @@ __device__ __forceinline__ void step_body(const kparams<T>& p)
         tl.nsrc = ns;
         tl.nrec = nr;
         tl.overflow = of;
+        // a mirror wall inside the window: point 0 or the point beyond the
+        // right end (index n_x)
+        tl.wall = (rd.k_left != 0.0 && w0 <= 0 && 0 < w1) ||
+            (rd.k_right != 0.0 && w0 <= (int64_t) rd.n_x && (int64_t) rd.n_x < w1);
     }
 
     T E[C], El[C], H[C], Hl[C], P[C];
