@@ -207,6 +207,16 @@ typedef struct mbg_tuning {
     uint32_t depth;
     uint32_t launches_per_graph; /* kernel launches captured in one CUDA graph */
     uint32_t staging;
+    uint32_t persistent; /* where the launch shape has a persistent
+                            kernel (2-level FP32 4 x 256, tensor-core 4-6
+                            levels): 1 = each advance runs its full launches
+                            as one persistent kernel (CTAs take the tiles of
+                            successive launches in order, each waiting for
+                            its neighbour tiles; bit-identical results),
+                            2 = one launch per `depth` steps in CUDA graphs,
+                            0 = automatic (persistent when a launch has
+                            fewer than 4 waves of tiles). The environment
+                            variable MBG_PERSISTENT=1 / =0 forces 1 / 2. */
 } mbg_tuning;
 
 /* ------------------------------------------------------------ entry points */

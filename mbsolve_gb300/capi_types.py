@@ -130,6 +130,7 @@ class mbg_tuning(C.Structure):
         ("depth", C.c_uint32),
         ("launches_per_graph", C.c_uint32),
         ("staging", C.c_uint32),
+        ("persistent", C.c_uint32),
     ]
 
 

@@ -132,6 +132,8 @@ int mbg_solver_run(mbg_solver* s)
         s->eng->advance(s->eng->steps_total());
         const uint32_t st = s->eng->status();
         if (st & mbg::STATUS_TC_WAIT) throw std::runtime_error("CUDA: a tensor-core completion wait ran out");
+        if (st & mbg::STATUS_PERSIST_WAIT)
+            throw std::runtime_error("CUDA: a persistent-kernel wait for neighbour tiles ran out");
     });
 }
 
@@ -292,6 +294,7 @@ int mbg_ensemble_info(const mbg_ensemble* e, uint64_t* cells, uint32_t* tiles, m
             t->depth = (uint32_t) u.depth;
             t->launches_per_graph = (uint32_t) u.graph;
             t->staging = (uint32_t) e->eng->staging();
+            t->persistent = (uint32_t) e->eng->persistent();
         }
     });
 }

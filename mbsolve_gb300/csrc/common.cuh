@@ -25,6 +25,7 @@ enum : uint32_t {
     STATUS_PRECOMPUTE = 2u,     // the FP64 precompute rejected a material
     STATUS_REGION = 4u,         // a grid point lies in no region
     STATUS_TC_WAIT = 8u,        // a tensor-core or bulk-copy completion wait ran out
+    STATUS_PERSIST_WAIT = 16u,  // a persistent-kernel wait for neighbour tiles ran out
 };
 
 // Per-tile work item: one contiguous output range of one run.
@@ -66,6 +67,17 @@ struct rec_desc {
     uint64_t rows;
     double ratio;        // interval ratio dt/interval (1 when every step)
     uint64_t offset;     // into the scratch of the run's records
+};
+
+// Schedule of one launch of the persistent time-step kernel (see
+// step_kernel_persist): `levels` launches' worth of tiles.
+struct persist_params {
+    uint32_t levels;     // levels (launches of nsub steps) in this launch
+    uint32_t n_tiles;
+    uint32_t base;       // levels every tile had finished before this launch
+    uint32_t* work;      // work counter, zero at the launch
+    uint32_t* prog;      // per tile: levels finished (absolute)
+    const int2* nb;      // per tile: left and right neighbour in its run (itself if none)
 };
 
 // Kernel-side record types beyond MBG_RECORD_*: a coherence record (the

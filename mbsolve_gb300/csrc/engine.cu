@@ -38,16 +38,16 @@ std::vector<kernel_entry<T> >& kernel_registry()
 }
 
 template<typename T>
-bool register_kernel(int algo, int lev, int C, int NT, launch_fn<T> fn, int staging)
+bool register_kernel(int algo, int lev, int C, int NT, launch_fn<T> fn, int staging, persist_fn<T> pfn)
 {
-    kernel_registry<T>().push_back(kernel_entry<T>{ algo, lev, C, NT, fn, staging });
+    kernel_registry<T>().push_back(kernel_entry<T>{ algo, lev, C, NT, fn, staging, pfn });
     return true;
 }
 
 template std::vector<kernel_entry<float> >& kernel_registry<float>();
 template std::vector<kernel_entry<double> >& kernel_registry<double>();
-template bool register_kernel<float>(int, int, int, int, launch_fn<float>, int);
-template bool register_kernel<double>(int, int, int, int, launch_fn<double>, int);
+template bool register_kernel<float>(int, int, int, int, launch_fn<float>, int, persist_fn<float>);
+template bool register_kernel<double>(int, int, int, int, launch_fn<double>, int, persist_fn<double>);
 
 // -------------------------------------------------------------- names
 
@@ -605,6 +605,7 @@ public:
     uint32_t tiles() const override { return (uint32_t) tiles_host_.size(); }
     tuning tuning_used() const override { return tune_; }
     int staging() const override { return staging_; }
+    int persistent() const override { return persist_; }
     void set_timing(bool on) override { timing_ = on; }
     void restart_clock() override { steps_done_ = 0; }
 
@@ -647,6 +648,15 @@ public:
         uint64_t full = steps / depth;
         const uint64_t rem = steps % depth;
         const uint32_t L = (uint32_t) tune_.graph;
+        if (persist_) {
+            // all full launches as persistent kernels (levels of one launch
+            // bounded so that the progress counters never wrap)
+            while (full) {
+                const uint32_t lv = (uint32_t) std::min<uint64_t>(full, 1u << 20);
+                launch_persistent(lv, (uint32_t) depth);
+                full -= lv;
+            }
+        }
         if (L >= 2) {
             while (full >= L) {
                 replay_graph();
@@ -811,6 +821,13 @@ private:
     dbuf<src_desc> srcs_;
     dbuf<rec_desc> recs_;
     dbuf<tile_desc> tiles_;
+    // persistent kernel: tile neighbours, per-tile progress, work counter,
+    // levels done since the tiles were built
+    dbuf<int2> nb_;
+    dbuf<uint32_t> prog_, work_;
+    uint32_t pbase_ = 0;
+    persist_fn<T> pfn_ = nullptr;
+    int persist_ = 0;
     dbuf<unsigned long long> step_, step_zero_;
     dbuf<uint32_t> status_;
     std::vector<tile_desc> tiles_host_;
@@ -1122,6 +1139,20 @@ private:
         const unsigned nt = (unsigned) tiles_host_.size();
         tile_uniform_kernel<<<(nt + 7) / 8, 256, 0, stream_>>>(tiles_.p, nt, runs_dev_.p, mat_.p, halo);
         MBG_CK(cudaGetLastError());
+        // persistent kernel: neighbours of each tile in its run, progress
+        // counters from zero
+        std::vector<int2> nb(nt);
+        for (unsigned i = 0; i < nt; i++) {
+            const bool l = i > 0 && tiles_host_[i - 1].run == tiles_host_[i].run;
+            const bool r = i + 1 < nt && tiles_host_[i + 1].run == tiles_host_[i].run;
+            nb[i] = make_int2(l ? (int) i - 1 : (int) i, r ? (int) i + 1 : (int) i);
+        }
+        nb_.alloc(std::max<size_t>(1, nt));
+        prog_.alloc(std::max<size_t>(1, nt));
+        MBG_CK(cudaMemcpyAsync(nb_.p, nb.data(), nt * sizeof(int2), cudaMemcpyHostToDevice, stream_));
+        MBG_CK(cudaMemsetAsync(prog_.p, 0, std::max<size_t>(1, nt) * sizeof(uint32_t), stream_));
+        if (!work_.p) work_.alloc(1);
+        pbase_ = 0;
         MBG_CK(cudaStreamSynchronize(stream_));
         for (int i = 0; i < 2; i++)
             if (graph_exec_[i]) {
@@ -1136,6 +1167,26 @@ private:
             if (e.algo == kind_.algo && e.lev == kind_.N && e.C == C && e.NT == NT && e.staging == staging_)
                 return e.fn;
         return nullptr;
+    }
+
+    persist_fn<T> find_persistent(int C, int NT) const
+    {
+        for (const auto& e : kernel_registry<T>())
+            if (e.algo == kind_.algo && e.lev == kind_.N && e.C == C && e.NT == NT && e.staging == 0)
+                return e.pfn;
+        return nullptr;
+    }
+
+    // MBG_PERSISTENT=1 / =0 force the persistent kernel on / off, as
+    // mbg_tuning.persistent = 1 / 2 do; otherwise -1 (automatic)
+    static int persistent_forced(const mbg_tuning* user)
+    {
+        if (user && user->persistent == 1) return 1;
+        if (user && user->persistent == 2) return 0;
+        const char* s = std::getenv("MBG_PERSISTENT");
+        if (s && s[0] == '1') return 1;
+        if (s && s[0] == '0') return 0;
+        return -1;
     }
 
     // MBG_TILE_STAGING=bulk selects the kernels that stage the tile state in
@@ -1218,6 +1269,40 @@ private:
         step_bump_kernel<<<1, 1, 0, stream_>>>(step_.p, (unsigned long long) count * nsub);
         MBG_CK(cudaGetLastError());
         launches_ += count + 1;
+    }
+
+    // `levels` launches of nsub steps as one persistent kernel
+    void launch_persistent(uint32_t levels, uint32_t nsub)
+    {
+        if ((uint64_t) pbase_ + levels >= (1ull << 31)) {
+            // progress counters near wrapping: start them again from zero
+            MBG_CK(cudaMemsetAsync(prog_.p, 0, prog_.n * sizeof(uint32_t), stream_));
+            pbase_ = 0;
+        }
+        ev_pair* ev = nullptr;
+        if (timing_) {
+            ev = &next_event();
+            ev->launches = levels;
+            MBG_CK(cudaEventRecord(ev->a, stream_));
+        }
+        MBG_CK(cudaMemsetAsync(work_.p, 0, sizeof(uint32_t), stream_));
+        persist_params q;
+        q.levels = levels;
+        q.n_tiles = (uint32_t) tiles_host_.size();
+        q.base = pbase_;
+        q.work = work_.p;
+        q.prog = prog_.p;
+        q.nb = nb_.p;
+        // level k reads buffer cur_ ^ (k & 1): the kernel flips odd levels
+        kparams<T> p = params(cur_, 0, nsub, true, step_.p);
+        pfn_(p, q, smem(), stream_);
+        MBG_CK(cudaGetLastError());
+        if (timing_) MBG_CK(cudaEventRecord(ev->b, stream_));
+        if (levels & 1u) cur_ = 1 - cur_;
+        pbase_ += levels;
+        step_bump_kernel<<<1, 1, 0, stream_>>>(step_.p, (unsigned long long) levels * nsub);
+        MBG_CK(cudaGetLastError());
+        launches_ += 3;
     }
 
     void replay_graph()
@@ -1422,7 +1507,24 @@ private:
             s << "no kernel instantiated for cells_per_thread=" << t.C << " threads=" << t.NT;
             throw invalid_argument(s.str());
         }
+        pfn_ = staging_ == 0 ? find_persistent(t.C, t.NT) : nullptr;
         build_tiles(t);
+        persist_ = 0;
+        if (pfn_) {
+            const int forced = persistent_forced(user);
+            if (forced >= 0) {
+                persist_ = forced;
+            } else {
+                // automatic: with few waves of tiles per launch the launch
+                // tails and the gaps between launches cost most (one
+                // 65,536-point 6-level run: 1.3 waves, 5.8e9 -> 8.4e9
+                // cell-updates/s persistent); with many the per-tile hand-off
+                // costs more than it saves (4,096 2-level runs: 12 % slower)
+                persist_params q{};
+                const unsigned slots = pfn_(params(cur_, 0, 1, false, step_zero_.p), q, smem(), stream_);
+                persist_ = tiles_host_.size() < 4ull * slots ? 1 : 0;
+            }
+        }
     }
 };
 

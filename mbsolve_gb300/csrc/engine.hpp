@@ -92,6 +92,7 @@ public:
     virtual uint32_t tiles() const = 0;
     virtual tuning tuning_used() const = 0;
     virtual int staging() const = 0;  // 0: registers, 1: bulk-copy staging
+    virtual int persistent() const = 0;  // 1: one persistent kernel per advance
     virtual void set_timing(bool on) = 0;
     virtual void kernel_time(uint64_t* launches, double* ms, bool reset) = 0;
     virtual uint32_t status() = 0;
@@ -128,17 +129,24 @@ void launch_precompute(
 template<typename T>
 using launch_fn = void (*)(const kparams<T>&, unsigned grid, size_t smem, cudaStream_t s);
 
+// the persistent kernel of a launch shape (step_kernel_persist); returns
+// the CTAs it runs with (q.levels == 0: only that number, no launch)
+template<typename T>
+using persist_fn = unsigned (*)(const kparams<T>&, const persist_params&, size_t smem, cudaStream_t s);
+
 template<typename T>
 struct kernel_entry {
     int algo, lev, C, NT;
     launch_fn<T> fn;
     int staging;  // 0: tile state loaded into registers, 1: bulk-copy (TMA) staging
+    persist_fn<T> pfn;  // null where the shape has no persistent kernel
 };
 
 template<typename T>
 std::vector<kernel_entry<T> >& kernel_registry();
 
 template<typename T>
-bool register_kernel(int algo, int lev, int C, int NT, launch_fn<T> fn, int staging = 0);
+bool register_kernel(int algo, int lev, int C, int NT, launch_fn<T> fn, int staging = 0,
+                     persist_fn<T> pfn = nullptr);
 
 }  // namespace mbg

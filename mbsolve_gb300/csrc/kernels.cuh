@@ -122,14 +122,16 @@ __device__ __forceinline__ void rot_coeffs<double>(double x, double& s, double& 
     }
 }
 
-template<typename T, int C>
+// CG: through L2 only (data another CTA of the same launch wrote);
+// otherwise streaming loads
+template<typename T, int C, bool CG = false>
 __device__ __forceinline__ void load_cells(T (&r)[C], const T* __restrict__ src, int64_t g0)
 {
     if constexpr (sizeof(T) == 4 && (C % 4) == 0) {
         const float4* s4 = reinterpret_cast<const float4*>(src + g0);
 #pragma unroll
         for (int q = 0; q < C / 4; q++) {
-            float4 v = __ldcs(s4 + q);
+            float4 v = CG ? __ldcg(s4 + q) : __ldcs(s4 + q);
             r[4 * q + 0] = v.x;
             r[4 * q + 1] = v.y;
             r[4 * q + 2] = v.z;
@@ -139,13 +141,13 @@ __device__ __forceinline__ void load_cells(T (&r)[C], const T* __restrict__ src,
         const double2* s2 = reinterpret_cast<const double2*>(src + g0);
 #pragma unroll
         for (int q = 0; q < C / 2; q++) {
-            double2 v = __ldcs(s2 + q);
+            double2 v = CG ? __ldcg(s2 + q) : __ldcs(s2 + q);
             r[2 * q + 0] = v.x;
             r[2 * q + 1] = v.y;
         }
     } else {
 #pragma unroll
-        for (int j = 0; j < C; j++) r[j] = __ldcs(src + g0 + j);
+        for (int j = 0; j < C; j++) r[j] = CG ? __ldcg(src + g0 + j) : __ldcs(src + g0 + j);
     }
 }
 

@@ -197,7 +197,7 @@ __device__ __forceinline__ bool tile_steps(
             // the coefficients are read here: values held in registers
             // across the time loop cost the 2-level kernel its register
             // budget (coefficients reloaded every step).
-            const run_desc& rw = p.runs[p.tiles[blockIdx.x].run];
+            const run_desc& rw = p.runs[td.run];
             const T k_left = (T) rw.k_left, k_right = (T) rw.k_right;
 #pragma unroll
             for (int j = 0; j < C; j++) {
@@ -335,10 +335,53 @@ __device__ __forceinline__ bool tile_steps(
     return true;
 }
 
-// One launch: every tile advances by nsub steps. TC: 4-6 levels in FP32
-// with the density products of uniform tiles on the tensor cores.
-template<typename T, int ALGO, int LEV, int C, int NT, bool TC, bool BULK = false>
-__device__ __forceinline__ void step_body(const kparams<T>& p)
+// Tensor memory columns, completion barrier and its phase of a CTA of the
+// tensor-core kernels (allocated once per CTA by the kernel wrappers).
+struct tc_res {
+    uint32_t tmem, mbar;
+    uint32_t* phase;  // shared: the barrier's phase between tiles
+};
+
+__device__ __forceinline__ tc_res tc_acquire(uint32_t* tmem_sh, uint64_t* mbar, uint32_t* phase_sh)
+{
+    if (threadIdx.x < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         (uint32_t) __cvta_generic_to_shared(tmem_sh)),
+                     "r"(tc::TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t) __cvta_generic_to_shared(mbar))
+                     : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *phase_sh = 0;
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    return tc_res{ *tmem_sh, (uint32_t) __cvta_generic_to_shared(mbar), phase_sh };
+}
+
+__device__ __forceinline__ void tc_release(const tc_res& r)
+{
+    tc::fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        tc::fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(r.tmem), "r"(tc::TMEM_COLS)
+                     : "memory");
+    }
+}
+
+// One tile of one launch: the tile advances by nsub steps. TC: 4-6 levels
+// in FP32 with the density products of uniform tiles on the tensor cores.
+// `flip` swaps the input and output buffers (odd levels of the persistent
+// kernel); CG loads the state through L2 only (the persistent kernel reads
+// what other CTAs of the same launch wrote).
+template<typename T, int ALGO, int LEV, int C, int NT, bool TC, bool BULK = false, bool CG = false>
+__device__ __forceinline__ void step_body(const kparams<T>& p, uint32_t tile, uint32_t launch_idx, bool flip,
+                                          const tc_res& res)
 {
     constexpr bool DF = sizeof(T) == 4;
     constexpr int D = density_len<ALGO, LEV>::value;
@@ -350,12 +393,24 @@ __device__ __forceinline__ void step_body(const kparams<T>& p)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sh_coef = reinterpret_cast<T*>(smem_raw);
 
-    const tile_desc td = p.tiles[blockIdx.x];
+    const tile_desc td = p.tiles[tile];
     const run_desc rd = p.runs[td.run];
     const int64_t l0 = (int64_t) td.out_start - (int64_t) p.halo + (int64_t) threadIdx.x * C;
     const int64_t g0 = (int64_t) rd.offset + l0;
     const int64_t nx = rd.n_x;
-    const uint64_t step0 = *p.step_base + (uint64_t) p.launch_idx * p.depth;
+    const uint64_t step0 = *p.step_base + (uint64_t) launch_idx * p.depth;
+    const T* const Ein = flip ? p.Eout : p.Ein;
+    const T* const Hin = flip ? p.Hout : p.Hin;
+    const T* const Pin = flip ? p.Pout : p.Pin;
+    const T* const Din = flip ? p.Dout : p.Din;
+    const T* const Elin = flip ? p.Elout : p.Elin;
+    const T* const Hlin = flip ? p.Hlout : p.Hlin;
+    T* const Eout = flip ? const_cast<T*>(p.Ein) : p.Eout;
+    T* const Hout = flip ? const_cast<T*>(p.Hin) : p.Hout;
+    T* const Pout = flip ? const_cast<T*>(p.Pin) : p.Pout;
+    T* const Dout = flip ? const_cast<T*>(p.Din) : p.Dout;
+    T* const Elout = flip ? const_cast<T*>(p.Elin) : p.Elout;
+    T* const Hlout = flip ? const_cast<T*>(p.Hlin) : p.Hlout;
     int nsteps = 0;
     if (step0 < rd.n_t) nsteps = (int) min((uint64_t) p.nsub, (uint64_t) rd.n_t - step0);
 
@@ -429,22 +484,22 @@ __device__ __forceinline__ void step_body(const kparams<T>& p)
             for (int j = 0; j < C; j++) Rl[j][v] = tmp[j];
         }
     } else {
-        load_cells<T, C>(E, p.Ein, g0);
-        load_cells<T, C>(H, p.Hin, g0);
-        load_cells<T, C>(P, p.Pin, g0);
+        load_cells<T, C, CG>(E, Ein, g0);
+        load_cells<T, C, CG>(H, Hin, g0);
+        load_cells<T, C, CG>(P, Pin, g0);
         if constexpr (DF) {
-            load_cells<T, C>(El, p.Elin, g0);
-            load_cells<T, C>(Hl, p.Hlin, g0);
+            load_cells<T, C, CG>(El, Elin, g0);
+            load_cells<T, C, CG>(Hl, Hlin, g0);
         }
         if constexpr (D > 0) {
 #pragma unroll
             for (int v = 0; v < D; v++) {
                 T tmp[C];
-                load_cells<T, C>(tmp, p.Din + (uint64_t) v * p.plane, g0);
+                load_cells<T, C, CG>(tmp, Din + (uint64_t) v * p.plane, g0);
 #pragma unroll
                 for (int j = 0; j < C; j++) R[j][v] = tmp[j];
                 if constexpr (DFD) {
-                    load_cells<T, C>(tmp, p.Din + (uint64_t) (D + v) * p.plane, g0);
+                    load_cells<T, C, CG>(tmp, Din + (uint64_t) (D + v) * p.plane, g0);
 #pragma unroll
                     for (int j = 0; j < C; j++) Rl[j][v] = tmp[j];
                 }
@@ -467,25 +522,7 @@ __device__ __forceinline__ void step_body(const kparams<T>& p)
         }
         if constexpr (!DF) El[j] = Hl[j] = T(0);
     }
-    // tensor memory and the completion barrier of the TC kernels
-    __shared__ __align__(8) uint64_t tc_mbar;
-    __shared__ uint32_t tc_tmem;
     tc::ctx tcc{};
-    if constexpr (TC) {
-        if (threadIdx.x < 32) {
-            asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                             (uint32_t) __cvta_generic_to_shared(&tc_tmem)),
-                         "r"(tc::TMEM_COLS)
-                         : "memory");
-            asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-        }
-        if (threadIdx.x == 0) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t) __cvta_generic_to_shared(&tc_mbar))
-                         : "memory");
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        }
-        tc::fence_before();
-    }
     const bool uniform = td.uniform_mat >= 0;
     if (uniform) {
         const T* src = p.mc + (uint64_t) td.uniform_mat * p.mstride;
@@ -515,9 +552,9 @@ __device__ __forceinline__ void step_body(const kparams<T>& p)
         tcc.b_hi = ops + 2u * TS::A_BYTES;
         tcc.b_lo = tcc.b_hi + TS::B_BYTES;
         tcc.b_dl = tcc.b_lo + TS::B_BYTES;
-        tcc.tmem = tc_tmem;
-        tcc.mbar = (uint32_t) __cvta_generic_to_shared(&tc_mbar);
-        tcc.phase = 0;
+        tcc.tmem = res.tmem;
+        tcc.mbar = res.mbar;
+        tcc.phase = *res.phase;
         if (uniform) tc::stage_b<D>(tcc, p.mc + (uint64_t) td.uniform_mat * p.mstride);
     }
 
@@ -531,14 +568,10 @@ __device__ __forceinline__ void step_body(const kparams<T>& p)
                                                sh_coef, tl, sh_a, sh_al, sh_b, sh_bl);
     }
     if constexpr (TC) {
-        tc::fence_before();
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            tc::fence_after();
-            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tcc.tmem),
-                         "r"(tc::TMEM_COLS)
-                         : "memory");
-        }
+        // every thread holds the same phase; the next tile of a persistent
+        // CTA continues from it (the barrier before its first product
+        // orders this write)
+        if (threadIdx.x == 0) *res.phase = tcc.phase;
     }
 
     // Cayley, FP32: renormalise the trace to that of the initial density
@@ -590,12 +623,12 @@ __device__ __forceinline__ void step_body(const kparams<T>& p)
         return;
     }
     const int64_t lo = td.out_start, hi = (int64_t) td.out_start + td.out_len;
-    store_cells<T, C>(E, p.Eout, g0, l0, lo, hi);
-    store_cells<T, C>(H, p.Hout, g0, l0, lo, hi);
-    store_cells<T, C>(P, p.Pout, g0, l0, lo, hi);
+    store_cells<T, C>(E, Eout, g0, l0, lo, hi);
+    store_cells<T, C>(H, Hout, g0, l0, lo, hi);
+    store_cells<T, C>(P, Pout, g0, l0, lo, hi);
     if constexpr (DF) {
-        store_cells<T, C>(El, p.Elout, g0, l0, lo, hi);
-        store_cells<T, C>(Hl, p.Hlout, g0, l0, lo, hi);
+        store_cells<T, C>(El, Elout, g0, l0, lo, hi);
+        store_cells<T, C>(Hl, Hlout, g0, l0, lo, hi);
     }
     if constexpr (D > 0) {
 #pragma unroll
@@ -603,11 +636,11 @@ __device__ __forceinline__ void step_body(const kparams<T>& p)
             T tmp[C];
 #pragma unroll
             for (int j = 0; j < C; j++) tmp[j] = R[j][v];
-            store_cells<T, C>(tmp, p.Dout + (uint64_t) v * p.plane, g0, l0, lo, hi);
+            store_cells<T, C>(tmp, Dout + (uint64_t) v * p.plane, g0, l0, lo, hi);
             if constexpr (DFD) {
 #pragma unroll
                 for (int j = 0; j < C; j++) tmp[j] = Rl[j][v];
-                store_cells<T, C>(tmp, p.Dout + (uint64_t) (D + v) * p.plane, g0, l0, lo, hi);
+                store_cells<T, C>(tmp, Dout + (uint64_t) (D + v) * p.plane, g0, l0, lo, hi);
             }
         }
     }
@@ -620,13 +653,17 @@ __device__ __forceinline__ void step_body(const kparams<T>& p)
 template<typename T, int ALGO, int LEV, int C, int NT>
 __global__ void __launch_bounds__(NT) step_kernel(const kparams<T> p)
 {
-    step_body<T, ALGO, LEV, C, NT, false>(p);
+    step_body<T, ALGO, LEV, C, NT, false>(p, blockIdx.x, p.launch_idx, false, tc_res{});
 }
 
 template<int LEV>
 __global__ void __launch_bounds__(tc::M, LEV <= 4 ? 4 : 3) step_kernel_tc(const kparams<float> p)
 {
-    step_body<float, 1, LEV, 1, tc::M, true>(p);
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_sh, phase_sh;
+    const tc_res r = tc_acquire(&tmem_sh, &mbar, &phase_sh);
+    step_body<float, 1, LEV, 1, tc::M, true>(p, blockIdx.x, p.launch_idx, false, r);
+    tc_release(r);
 }
 
 // 2-level FP32 kernels with bulk-copy (TMA) staging of the tile state; not
@@ -635,7 +672,98 @@ __global__ void __launch_bounds__(tc::M, LEV <= 4 ? 4 : 3) step_kernel_tc(const 
 template<int C, int NT>
 __global__ void __launch_bounds__(NT) step_kernel_bulk(const kparams<float> p)
 {
-    step_body<float, 1, 2, C, NT, false, true>(p);
+    step_body<float, 1, 2, C, NT, false, true>(p, blockIdx.x, p.launch_idx, false, tc_res{});
+}
+
+// ------------------------------------------------------- persistent kernel
+//
+// One launch runs q.levels launches' worth of tiles ("levels" of nsub
+// steps). The CTAs take work items w = level * n_tiles + tile from a
+// global counter, in order, until none is left. A tile of
+// level k reads what its own tile and its two neighbours (the only tiles
+// whose outputs its window overlaps: a halo is at most half an output
+// range) wrote at level k - 1, and overwrites a buffer those three read at
+// level k - 1: it waits until all three have finished level k - 1
+// (per-tile progress counters, absolute over the launches so that nothing
+// is reset between launches). Items are taken in order, so every item
+// waited for was taken earlier by a running CTA (a CTA takes items only
+// while it runs) and finishes: no deadlock, whether or not every CTA of the
+// grid is resident at once. Waits are bounded; a time-out sets STATUS_PERSIST_WAIT.
+// Results equal the launch-per-level kernels' bit for bit (same tiles,
+// same arithmetic); what goes away is the wave quantisation and the gaps
+// between launches (long single runs have only 1-3 waves of tiles).
+
+constexpr uint32_t PERSIST_WAIT_LIMIT = 1u << 24;
+
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* a)
+{
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
+    return v;
+}
+
+// until the three progress counters reach `need` (polled together), then
+// an acquire fence; false when the wait ran out
+__device__ __forceinline__ bool wait_progress(const uint32_t* a, const uint32_t* b, const uint32_t* c,
+                                              uint32_t need)
+{
+    for (uint32_t it = 0; it < PERSIST_WAIT_LIMIT; it++) {
+        const uint32_t va = ld_relaxed(a), vb = ld_relaxed(b), vc = ld_relaxed(c);
+        if ((int32_t) (va - need) >= 0 && (int32_t) (vb - need) >= 0 && (int32_t) (vc - need) >= 0) {
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
+            return true;
+        }
+        __nanosleep(32);
+    }
+    return false;
+}
+
+template<typename T, int ALGO, int LEV, int C, int NT, bool TC>
+__device__ __forceinline__ void persist_loop(const kparams<T>& p, const persist_params& q, const tc_res& r)
+{
+    __shared__ uint32_t w_sh;
+    const uint32_t total = q.levels * q.n_tiles;
+    if (threadIdx.x == 0) w_sh = atomicAdd(q.work, 1u);
+    __syncthreads();
+    for (;;) {
+        const uint32_t w = w_sh;
+        if (w >= total) break;  // the same in every thread
+        const uint32_t k = w / q.n_tiles, i = w - k * q.n_tiles;
+        if (threadIdx.x == 0) {
+            const int2 nb = q.nb[i];
+            if (!wait_progress(q.prog + i, q.prog + nb.x, q.prog + nb.y, q.base + k))
+                atomicOr(p.status, STATUS_PERSIST_WAIT);
+        }
+        __syncthreads();
+        step_body<T, ALGO, LEV, C, NT, TC, false, true>(p, i, k, (k & 1u) != 0, r);
+        // the CTA's stores, then (one thread) a release fence and the
+        // progress mark; the next item is fetched meanwhile
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(q.prog + i), "r"(q.base + k + 1)
+                         : "memory");
+            w_sh = atomicAdd(q.work, 1u);
+        }
+        __syncthreads();
+    }
+}
+
+template<typename T, int ALGO, int LEV, int C, int NT>
+__global__ void __launch_bounds__(NT) step_kernel_persist(const kparams<T> p, const persist_params q)
+{
+    persist_loop<T, ALGO, LEV, C, NT, false>(p, q, tc_res{});
+}
+
+template<int LEV>
+__global__ void __launch_bounds__(tc::M, LEV <= 4 ? 4 : 3)
+    step_kernel_persist_tc(const kparams<float> p, const persist_params q)
+{
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_sh, phase_sh;
+    const tc_res r = tc_acquire(&tmem_sh, &mbar, &phase_sh);
+    persist_loop<float, 1, LEV, 1, tc::M, true>(p, q, r);
+    tc_release(r);
 }
 
 }  // namespace mbg

@@ -70,7 +70,7 @@ class ensemble:
         return dict(cells=cells.value, tiles=tiles.value,
                     cells_per_thread=t.cells_per_thread, threads=t.threads,
                     depth=t.depth, launches_per_graph=t.launches_per_graph,
-                    staging=t.staging)
+                    staging=t.staging, persistent=t.persistent)
 
     def results(self, run):
         out = []
@@ -164,11 +164,14 @@ class ensemble:
 
 
 def tuning(cells_per_thread=0, threads=0, depth=0, launches_per_graph=0,
-           staging=0):
+           staging=0, persistent=0):
     """Launch shape (0 = autotuned); staging 1 = bulk-copy (TMA) staging of
-    the tile state (2-level FP32)."""
+    the tile state (2-level FP32); persistent 1 = one persistent kernel per
+    advance where the launch shape has one, 2 = one launch per level, 0 =
+    automatic (persistent when a launch has few waves of tiles)."""
     t = T.mbg_tuning()
     t.staging = staging
+    t.persistent = persistent
     t.cells_per_thread = cells_per_thread
     t.threads = threads
     t.depth = depth

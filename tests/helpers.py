@@ -92,8 +92,9 @@ def plane_basis_step(c, L, d, e):
     return Q @ u2, c[L["p0"]] + g @ v2
 
 
-def tuning(C_=0, NT=0, depth=0, graph=0):
+def tuning(C_=0, NT=0, depth=0, graph=0, persistent=0):
     t = T.mbg_tuning()
+    t.persistent = persistent
     t.cells_per_thread = C_
     t.threads = NT
     t.depth = depth

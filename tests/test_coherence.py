@@ -177,3 +177,22 @@ def test_gpu_plain_offdiagonal_record_stays_zero(native):
     got = _gpu_complex("gpu-fdtd-2lvl-cvr-rodr-fp64", dev, sce)
     assert np.abs(got[3]).max() == 0.0
     assert np.abs(got[1]).max() > 0.4
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("algo,prec,tol", [
+    ("cvr-rodr", "fp64", 1e-9), ("reg-cayley", "fp64", 1e-9),
+    ("cvr-rodr", "fp32", 2e-5), ("reg-cayley", "fp32", 1e-4)])
+def test_gpu_bloch_norm_drift(native, algo, prec, tol):
+    """Bloch-norm drift of an undamped 2-level point over a pulse (20,000
+    steps): |4 |rho_12|^2 + w^2 - 1|, zero for the exact pure state. The
+    FP32 coherence vector is a float pair (measured below 2e-5); the FP32
+    Cayley matrix is plain FP32, renormalised in trace only (measured
+    2.9e-5)."""
+    got = _gpu_complex("gpu-fdtd-2lvl-%s-%s" % (algo, prec), *_rabi())
+    w = got[0].real[:, 0]
+    r = got[1][:, 0]
+    assert np.abs(r).max() > 0.4
+    drift = np.abs(4 * np.abs(r) ** 2 + w ** 2 - 1.0).max()
+    print(algo, prec, "Bloch-norm drift %.2e" % drift)
+    assert drift < tol
