@@ -209,7 +209,8 @@ typedef struct mbg_tuning {
     uint32_t staging;
     uint32_t persistent; /* where the launch shape has a persistent
                             kernel (2-level FP32 4 x 256, tensor-core 4-6
-                            levels): 1 = each advance runs its full launches
+                            levels, FP32 Cayley 4-6 levels): 1 = each
+                            advance runs its full launches
                             as one persistent kernel (CTAs take the tiles of
                             successive launches in order, each waiting for
                             its neighbour tiles; bit-identical results),

@@ -1164,15 +1164,17 @@ private:
     launch_fn<T> find_kernel(int C, int NT) const
     {
         for (const auto& e : kernel_registry<T>())
-            if (e.algo == kind_.algo && e.lev == kind_.N && e.C == C && e.NT == NT && e.staging == staging_)
+            if (e.algo == kind_.algo && e.lev == kind_.N && e.C == C && e.NT == NT && e.staging == staging_ && e.fn)
                 return e.fn;
         return nullptr;
     }
 
+    // a shape may be registered twice (its persistent kernel compiled in a
+    // translation unit of its own): the first entry with one
     persist_fn<T> find_persistent(int C, int NT) const
     {
         for (const auto& e : kernel_registry<T>())
-            if (e.algo == kind_.algo && e.lev == kind_.N && e.C == C && e.NT == NT && e.staging == 0)
+            if (e.algo == kind_.algo && e.lev == kind_.N && e.C == C && e.NT == NT && e.staging == 0 && e.pfn)
                 return e.pfn;
         return nullptr;
     }
@@ -1476,7 +1478,7 @@ private:
                 // (each stage ends with a run-off of its close contenders)
                 std::vector<std::pair<tuning, double> > shapes;
                 for (const auto& e : kernel_registry<T>()) {
-                    if (e.algo != kind_.algo || e.lev != kind_.N || e.staging != staging_) continue;
+                    if (e.algo != kind_.algo || e.lev != kind_.N || e.staging != staging_ || !e.fn) continue;
                     tuning c = t;
                     c.C = e.C;
                     c.NT = e.NT;

@@ -122,6 +122,11 @@ unsigned launch_persist_tc(const kparams<float>& p, const persist_params& q, siz
     static const bool MBG_CAT(mbg_reg_, __LINE__) = ::mbg::register_kernel<float>( \
         ::mbg::ALGO_CVR, LEV, 1, ::mbg::tc::M, &::mbg::launch_step_tc<LEV>, 0,      \
         &::mbg::launch_persist_tc<LEV>);
+// only the persistent kernel of a shape registered elsewhere (a
+// translation unit of its own, so that no kernel is compiled twice)
+#define MBG_REG_CAY_PONLY(T, LEV, C, NT)                                       \
+    static const bool MBG_CAT(mbg_reg_, __LINE__) = ::mbg::register_kernel<T>( \
+        ::mbg::ALGO_CAYLEY, LEV, C, NT, nullptr, 0, &::mbg::launch_persist<T, 2, LEV, C, NT>);
 #define MBG_REG_CVR_P(T, LEV, C, NT)                                           \
     static const bool MBG_CAT(mbg_reg_, __LINE__) = ::mbg::register_kernel<T>( \
         ::mbg::ALGO_CVR, LEV, C, NT, &::mbg::launch_step<T, 1, LEV, C, NT>, 0,  \

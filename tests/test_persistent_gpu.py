@@ -72,6 +72,24 @@ def test_persistent_tensor_core_equals_launch_per_level(native, levels):
             assert np.array_equal(np.asarray(x), np.asarray(y))
 
 
+@pytest.mark.parametrize("levels", [4, 6])
+def test_persistent_cayley_equals_launch_per_level(native, levels):
+    name = "gpu-fdtd-%dlvl-reg-cayley-fp32" % levels
+
+    def pairs():
+        mb.material.clear_library()
+        return [setups.random_nlvl(N=levels, num_gridpoints=n,
+                                   num_timesteps=300, seed=s, e_seed=3e7)
+                for n, s in ((6000, 3), (300, 4))]
+
+    _, ref = _run(name, pairs(), helpers.tuning(1, 128, 8, 8, 2), [77])
+    ens, got = _run(name, pairs(), helpers.tuning(1, 128, 8, 8, 1), [77])
+    assert ens.info()["persistent"] == 1
+    for a, b in zip(got, ref):
+        for x, y in zip(a, b):
+            assert np.array_equal(np.asarray(x), np.asarray(y))
+
+
 def test_persistent_is_chosen_for_few_tiles(native):
     """Automatic choice: a short single run (a few tiles per launch) takes
     the persistent kernel, a wide ensemble the launch per level."""
