@@ -79,6 +79,24 @@ def test_oracle_matches_reference_live(solver, setup, kw):
         np.testing.assert_allclose(a, b, rtol=0, atol=1e-12 * max(1.0, np.abs(b).max()))
 
 
+@pytest.mark.skipif(not _ref_available(), reason="reference tree not present")
+@pytest.mark.parametrize("algo", ["cvr-rodr", "reg-cayley"])
+def test_reference_plain_and_red_loops_agree(algo):
+    """The reference's two CPU time loops, solver_cpu_fdtd and the
+    temporally blocked solver_cpu_fdtd_red, give the same probe E bit for
+    bit (the oracle restates the plain one; the CPU baseline times it)."""
+    out = []
+    for name in ("cpu-fdtd-2lvl-" + algo, "cpu-fdtd-red-2lvl-" + algo):
+        mb.material.clear_library()
+        dev, sce = helpers.build_setup(
+            {"setup": "sit_2lvl", "kw": dict(num_gridpoints=1024,
+                                             num_timesteps=3000)})
+        _, r = helpers.reference_results(name, dev, sce)
+        out.append(r[0])
+    assert np.abs(out[0]).max() > 1.0
+    assert np.array_equal(out[0], out[1])
+
+
 # ---------------------------------------------- algebra vs numpy / scipy
 
 def test_expm_matches_scipy():
