@@ -451,7 +451,10 @@ __device__ __forceinline__ void cvr_update_df(float (&uh)[V], float (&ul)[V], fl
     pout = pp;
 }
 
-// Value of a record at one point (solver_cpu_fdtd.tpp:301-325).
+// Value of a record at one point (solver_cpu_fdtd.tpp:301-325), on the
+// kernels' state z (the coherence vector half a step ahead, see
+// cvr_layout); REC_COH_RE / REC_COH_IM: the parts of a coherence record
+// (no reference counterpart).
 template<typename T, int V>
 __device__ __forceinline__ T cvr_record_value(
     const rec_desc& rc,
@@ -505,21 +508,6 @@ __device__ __forceinline__ T cvr_record_value(
         return (rc.type == REC_COH_IM && rc.row_idx > rc.col_idx) ? -s : s;
     }
 }
-
-template<typename T>
-__device__ __forceinline__ void store_record(
-    const kparams<T>& p,
-    const rec_desc& rc,
-    uint64_t n,
-    int64_t l,
-    T v)
-{
-    uint64_t row = (uint64_t) floor(rc.ratio * (double) n);
-    if (row >= rc.rows) return;
-    p.scratch[rc.offset + row * rc.cols + (uint64_t) (l - rc.pos)] = v;
-    if (!isfinite(v)) atomicOr(p.status, STATUS_NONFINITE);
-}
-
 
 // ------------------------------------------------------- field updates
 
