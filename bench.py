@@ -190,19 +190,31 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(cells, depth):
+def ncu_traffic(cells, width, depth):
     """DRAM bytes per launch of the tile kernel from the committed ncu
-    summary (captured on a smaller ensemble and scaled by cells when the
-    depth matches), or None."""
+    capture (a smaller ensemble at tile width 1024, depth 32), scaled to
+    this launch: writes by the points (each output point once), reads by
+    the points and the tile's window over its output range (width /
+    (width - 2 halo), halo = depth rounded up to 8). Returns (bytes, how)
+    or (None, why)."""
     path = os.path.join(ROOT, "profiles", "tile_kernel_fp32_2lvl_traffic.json")
     try:
         with open(path) as f:
             d = json.load(f)
-        if int(d.get("depth", -1)) != int(depth):
-            return None
-        return float(d["dram_bytes_per_launch"]) * cells / float(d["cells"])
-    except Exception:
-        return None
+        halo = lambda dep: (int(dep) + 7) // 8 * 8
+        w0, h0 = 1024, halo(d["depth"])
+        h = halo(depth)
+        if width - 2 * h <= 0:
+            return None, "tile narrower than its halos"
+        scale = cells / float(d["cells"])
+        win = (width / float(width - 2 * h)) / (w0 / float(w0 - 2 * h0))
+        b = (float(d["dram_read_bytes"]) * win + float(d["dram_write_bytes"])) * scale
+        how = ("ncu capture at width %d, depth %d scaled by points" % (w0, d["depth"]))
+        if int(d["depth"]) != int(depth) or width != w0:
+            how += " and by the window/output ratio of width %d, depth %d" % (width, depth)
+        return b, how
+    except Exception as e:
+        return None, "no ncu capture (%s)" % e
 
 
 # --------------------------------------------------------- CPU baseline
@@ -415,7 +427,8 @@ def run_ours(args, dist):
     achieved = alg_bytes / t_launch / 1e9
     # state moved once per launch: the unavoidable bytes with blocking
     blocked_bytes = BYTES_PER_CELL_UPDATE_FP32 * cells
-    traffic = ncu_traffic(cells, depth)
+    traffic, traffic_how = ncu_traffic(
+        cells, info["cells_per_thread"] * info["threads"], depth)
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
         "frac": achieved / hbm, "traffic": traffic,
@@ -430,6 +443,7 @@ def run_ours(args, dist):
         "state_gbs": blocked_bytes / t_launch / 1e9,
         "state_frac": blocked_bytes / t_launch / 1e9 / hbm,
         "dram_gbs": (traffic / t_launch / 1e9) if traffic else None,
+        "traffic_source": traffic_how,
         "note": "achieved counts 88 B per cell-update (one unblocked pass) x "
                 "cells x depth per launch; with temporal blocking the state "
                 "crosses HBM once per launch (state_gbs), so achieved may "

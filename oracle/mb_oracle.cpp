@@ -30,7 +30,7 @@
  *   linear solves: Gaussian elimination with full pivoting (in place of
  *     FullPivLU) and Gauss-Jordan with partial pivoting (in place of
  *     inverse()).
- * Deviations from the reference, all documented in the design doc: a soft source
+ * Deliberate deviations from the reference: a soft source
  * is applied once per step (the reference applies it once per OpenMP
  * thread, solver_cpu_fdtd.tpp:245-255); the 2-level closed form guards
  * theta_1 = 0 (the reference divides by zero there).
