@@ -649,10 +649,12 @@ public:
         const uint64_t rem = steps % depth;
         const uint32_t L = (uint32_t) tune_.graph;
         if (persist_) {
-            // all full launches as persistent kernels (levels of one launch
-            // bounded so that the progress counters never wrap)
+            // all full launches as persistent kernels; the levels of one
+            // launch bounded so that its work items (levels x tiles, 32-bit
+            // in the kernel) and the progress counters stay below 2^31
+            const uint64_t per = std::max<uint64_t>(1, ((1ull << 31) - 1) / std::max<size_t>(1, tiles_host_.size()));
             while (full) {
-                const uint32_t lv = (uint32_t) std::min<uint64_t>(full, 1u << 20);
+                const uint32_t lv = (uint32_t) std::min<uint64_t>(std::min<uint64_t>(full, per), 1u << 20);
                 launch_persistent(lv, (uint32_t) depth);
                 full -= lv;
             }
