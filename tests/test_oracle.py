@@ -57,6 +57,20 @@ def _ref_available():
      dict(N=3, num_gridpoints=128, num_timesteps=300)),
     ("cpu-fdtd-4lvl-reg-cayley", "random_nlvl",
      dict(N=4, num_gridpoints=128, num_timesteps=300)),
+    ("cpu-fdtd-2lvl-reg-cayley", "random_nlvl",
+     dict(N=2, num_gridpoints=96, num_timesteps=300, e_seed=3e7)),
+    ("cpu-fdtd-3lvl-reg-cayley", "random_nlvl",
+     dict(N=3, num_gridpoints=96, num_timesteps=300, e_seed=3e7)),
+    ("cpu-fdtd-4lvl-cvr-rodr", "random_nlvl",
+     dict(N=4, num_gridpoints=96, num_timesteps=300, e_seed=3e7)),
+    ("cpu-fdtd-5lvl-cvr-rodr", "random_nlvl",
+     dict(N=5, num_gridpoints=64, num_timesteps=200, e_seed=3e7)),
+    ("cpu-fdtd-5lvl-reg-cayley", "random_nlvl",
+     dict(N=5, num_gridpoints=64, num_timesteps=200, e_seed=3e7)),
+    ("cpu-fdtd-6lvl-cvr-rodr", "random_nlvl",
+     dict(N=6, num_gridpoints=64, num_timesteps=200, e_seed=3e7)),
+    ("cpu-fdtd-6lvl-reg-cayley", "random_nlvl",
+     dict(N=6, num_gridpoints=64, num_timesteps=200, e_seed=3e7)),
 ])
 def test_oracle_matches_reference_live(solver, setup, kw):
     """Fresh setups (random E initial field, two materials, H record at an
