@@ -16,6 +16,8 @@
  *   internal/algo_lindblad_noop.hpp:35-86        Maxwell only
  *   internal/copy_list_entry.hpp:51-229  recording plan
  *   solver-cpu/.../solver_cpu_fdtd.tpp:36-338    constructor and run()
+ *   solver-cpu/.../solver_cpu_fdtd_red.tpp:351-567  the temporally blocked
+ *                                        loop (run_red; same results)
  *   qm_description.hpp:166-236           Lindblad relaxation action
  *   source.hpp:94-106,190-194,256-260    source waveforms
  * The reference leans on Eigen for three numerical kernels; this file has
@@ -1217,36 +1219,55 @@ static solver* create(
 }
 
 /* rho[row][col] of a coherence record at point i (see cvr_coherence) */
-static cplx coherence_value(const solver* s, const record_plan& rp, uint64_t i)
+/* The state a record reads: the solver's arrays, or a thread's private
+ * copy of a range of them (grid point i at index i - base). */
+struct view {
+    const real* e;
+    const real* h;
+    const real* p;
+    const real* d_cvr;
+    const cmat* d_cay;
+    int64_t base;
+};
+
+static view full_view(const solver* s)
 {
+    return view{ s->e.data(), s->h.data(), s->p.data(), s->d_cvr.data(), s->d_cay.data(), 0 };
+}
+
+/* rho[row][col] of a coherence record at point i (see cvr_coherence) */
+static cplx coherence_value(const solver* s, const view& w, const record_plan& rp, uint64_t i)
+{
+    const int64_t k = (int64_t) i - w.base;
     if (s->algo == ALGO_RODR)
-        return cvr_coherence(s->N, &s->d_cvr[i * s->V], rp.row_idx, rp.col_idx);
-    if (s->algo == ALGO_CAYLEY) return s->d_cay[i](rp.row_idx, rp.col_idx);
+        return cvr_coherence(s->N, &w.d_cvr[k * s->V], rp.row_idx, rp.col_idx);
+    if (s->algo == ALGO_CAYLEY) return w.d_cay[k](rp.row_idx, rp.col_idx);
     return cplx(0.0, 0.0);
 }
 
-static real record_value(const solver* s, const record_plan& rp, uint64_t i)
+static real record_value(const solver* s, const view& w, const record_plan& rp, uint64_t i)
 {
-    if (rp.coherence) return coherence_value(s, rp, i).real();
+    if (rp.coherence) return coherence_value(s, w, rp, i).real();
+    const int64_t k = (int64_t) i - w.base;
     switch (rp.type) {
     case MBG_RECORD_ELECTRIC:
-        return s->e[i];
+        return w.e[k];
     case MBG_RECORD_POLAR_DT:
-        return s->p[i];
+        return w.p[k];
     case MBG_RECORD_MAGNETIC:
-        return s->h[i];
+        return w.h[k];
     case MBG_RECORD_INVERSION:
         if (s->algo == ALGO_RODR)
-            return s->d_cvr[i * s->V + s->N * (s->N - 1)];
+            return w.d_cvr[k * s->V + s->N * (s->N - 1)];
         if (s->algo == ALGO_CAYLEY)
-            return (s->d_cay[i](1, 1) - s->d_cay[i](0, 0)).real();
+            return (w.d_cay[k](1, 1) - w.d_cay[k](0, 0)).real();
         return 0.0;
     case MBG_RECORD_DENSITY:
         if (rp.row_idx != rp.col_idx) return 0.0; /* coherences: TODO in ref */
         if (s->algo == ALGO_RODR)
-            return cvr_population(s->N, &s->d_cvr[i * s->V], rp.row_idx);
+            return cvr_population(s->N, &w.d_cvr[k * s->V], rp.row_idx);
         if (s->algo == ALGO_CAYLEY)
-            return s->d_cay[i](rp.row_idx, rp.row_idx).real();
+            return w.d_cay[k](rp.row_idx, rp.row_idx).real();
         return 0.0;
     default:
         return 0.0;
@@ -1306,16 +1327,122 @@ static void run(solver* s, int threads, uint32_t max_steps)
                 int64_t o_r = rp.offset(t);
                 if ((uint64_t) (o_r - (int64_t) rp.offset_real) >= rp.rows * cols)
                     continue; /* row outside the result (guard) */
+                const view w = full_view(s);
 #pragma omp for schedule(static)
                 for (int64_t i = (int64_t) pos; i < (int64_t) (pos + cols); i++)
-                    if (i < n) s->scratch[o_r + i - pos] = record_value(s, rp, i);
+                    if (i < n) s->scratch[o_r + i - pos] = record_value(s, w, rp, i);
                 if (rp.coherence) {
                     int64_t o_i = o_r - (int64_t) rp.offset_real + (int64_t) rp.offset_imag;
 #pragma omp for schedule(static)
                     for (int64_t i = (int64_t) pos; i < (int64_t) (pos + cols); i++)
-                        if (i < n) s->scratch[o_i + i - pos] = coherence_value(s, rp, i).imag();
+                        if (i < n) s->scratch[o_i + i - pos] = coherence_value(s, w, rp, i).imag();
                 }
             }
+        }
+    }
+    s->steps_done += steps;
+}
+
+/* solver_cpu_fdtd_red::run (red.tpp:351-567) restated: each thread owns a
+ * contiguous range of points and, every `ol` steps, copies that range
+ * widened by ol points on each side into private arrays, advances the
+ * copy by up to ol steps, and writes its own range back. Garbage enters a
+ * copy from its open edges by one point per step, so the owned range stays
+ * exact; the arithmetic of every point and step is that of run() (same
+ * order: E, sources, H and boundary, density, records), so the results
+ * equal run()'s bit for bit. Two barriers per ol steps instead of several
+ * per step: the loop for small runs on many cores. Falls back to run()
+ * when a thread would own fewer than 2 ol points. */
+static void run_red(solver* s, int threads, uint32_t max_steps, int ol)
+{
+    const int64_t n = s->n_x;
+    uint32_t steps = s->n_t;
+    if (max_steps && max_steps < steps) steps = max_steps;
+    if (threads < 1) threads = 1;
+    if (ol < 1) ol = 1;
+    if (n < (int64_t) threads * 2 * ol) {
+        run(s, threads, max_steps);
+        return;
+    }
+    const int V = s->V;
+    const real dxi = s->dx_inv;
+#pragma omp parallel num_threads(threads)
+    {
+        const int t = omp_get_thread_num();
+        const int nt = omp_get_num_threads();
+        const int64_t chunk = n / nt;
+        const int64_t b = t * chunk, e = (t == nt - 1) ? n : b + chunk;
+        const int64_t lo = std::max<int64_t>(0, b - ol), hi = std::min<int64_t>(n, e + ol);
+        const int64_t m = hi - lo;
+        std::vector<real> E(m), H(m + 1), P(m), D(s->algo == ALGO_RODR ? (size_t) m * V : 0);
+        std::vector<cmat> R(s->algo == ALGO_CAYLEY ? m : 0);
+        const view w{ E.data(), H.data(), P.data(), D.data(), R.data(), lo };
+        for (uint32_t t0 = 0; t0 < steps; t0 += (uint32_t) ol) {
+            const uint32_t nsub = std::min<uint32_t>((uint32_t) ol, steps - t0);
+            std::copy(s->e.begin() + lo, s->e.begin() + hi, E.begin());
+            std::copy(s->h.begin() + lo, s->h.begin() + hi + 1, H.begin());
+            std::copy(s->p.begin() + lo, s->p.begin() + hi, P.begin());
+            if (s->algo == ALGO_RODR)
+                std::copy(s->d_cvr.begin() + lo * V, s->d_cvr.begin() + hi * V, D.begin());
+            else if (s->algo == ALGO_CAYLEY)
+                std::copy(s->d_cay.begin() + lo, s->d_cay.begin() + hi, R.begin());
+#pragma omp barrier
+            // local pointers shifted to the copy's first point, as run()'s
+            // plain arrays (so that the loops vectorise alike)
+            real* __restrict__ Ep = E.data();
+            real* __restrict__ Hp = H.data();
+            real* __restrict__ Pp = P.data();
+            const real* __restrict__ fa = s->fac_a.data() + lo;
+            const real* __restrict__ fb = s->fac_b.data() + lo;
+            const real* __restrict__ fc = s->fac_c.data() + lo;
+            const real* __restrict__ ga = s->gamma.data() + lo;
+            const uint32_t* mi = s->mat_idx.data() + lo;
+            for (uint32_t k = 0; k < nsub; k++) {
+                const uint32_t step = t0 + k;
+                for (int64_t i = 0; i < m; i++)
+                    Ep[i] = fa[i] * Ep[i] + fb[i] * (-ga[i] * Pp[i] + (Hp[i + 1] - Hp[i]) * dxi);
+                for (const auto& src : s->sources) {
+                    const int64_t x = src.x_idx;
+                    if (x < lo || x >= hi) continue;
+                    if (src.type == MBG_SOURCE_HARD)
+                        Ep[x - lo] = src.values[step];
+                    else if (src.type == MBG_SOURCE_SOFT)
+                        Ep[x - lo] += src.values[step];
+                }
+                for (int64_t i = 1; i < m; i++) Hp[i] += fc[i] * (Ep[i] - Ep[i - 1]);
+                if (lo == 0) Hp[0] = s->wall_l != 0 ? s->wall_l * Ep[0] : 0;
+                if (hi == n) Hp[m] = s->wall_r != 0 ? -s->wall_r * Ep[m - 1] : 0;
+                if (s->algo == ALGO_RODR) {
+                    for (int64_t i = 0; i < m; i++)
+                        rodr_update(s->rodr[mi[i]], s->N, &D[i * V], Ep[i], &Pp[i]);
+                } else if (s->algo == ALGO_CAYLEY) {
+                    for (int64_t i = 0; i < m; i++)
+                        cayley_update(s->cay[mi[i]], R[i], Ep[i], &Pp[i]);
+                }
+                for (const auto& rp : s->records) {
+                    if (!rp.hasto_record(step)) continue;
+                    const int64_t pos = (int64_t) rp.position_idx, cols = (int64_t) rp.cols;
+                    const int64_t o_r = rp.offset(step);
+                    if ((uint64_t) (o_r - (int64_t) rp.offset_real) >= rp.rows * rp.cols) continue;
+                    const int64_t r0 = std::max(pos, b), r1 = std::min(pos + cols, e);
+                    for (int64_t i = r0; i < r1; i++) {
+                        s->scratch[o_r + i - pos] = record_value(s, w, rp, i);
+                        if (rp.coherence)
+                            s->scratch[o_r - (int64_t) rp.offset_real + (int64_t) rp.offset_imag + i - pos] =
+                                coherence_value(s, w, rp, i).imag();
+                    }
+                }
+            }
+            // the owned range back; H at the owned points (and H[n] for the
+            // last range)
+            std::copy(E.begin() + (b - lo), E.begin() + (e - lo), s->e.begin() + b);
+            std::copy(H.begin() + (b - lo), H.begin() + (e - lo) + (e == n ? 1 : 0), s->h.begin() + b);
+            std::copy(P.begin() + (b - lo), P.begin() + (e - lo), s->p.begin() + b);
+            if (s->algo == ALGO_RODR)
+                std::copy(D.begin() + (b - lo) * V, D.begin() + (e - lo) * V, s->d_cvr.begin() + b * V);
+            else if (s->algo == ALGO_CAYLEY)
+                std::copy(R.begin() + (b - lo), R.begin() + (e - lo), s->d_cay.begin() + b);
+#pragma omp barrier
         }
     }
     s->steps_done += steps;
@@ -1383,6 +1510,12 @@ int mbo_grid(const mbo_solver* h, mbg_grid* g)
 int mbo_run(mbo_solver* h, int threads, uint32_t max_steps)
 {
     return guard([&] { mbo::run((mbo::solver*) h, threads, max_steps); });
+}
+
+/* the temporally blocked loop (solver_cpu_fdtd_red), overlap `ol` steps */
+int mbo_run_red(mbo_solver* h, int threads, uint32_t max_steps, int ol)
+{
+    return guard([&] { mbo::run_red((mbo::solver*) h, threads, max_steps, ol); });
 }
 
 int mbo_num_results(const mbo_solver* h, uint32_t* n)

@@ -29,6 +29,7 @@ def lib():
                                  C.POINTER(C.c_void_p)]
         L.mbo_grid.argtypes = [C.c_void_p, C.POINTER(T.mbg_grid)]
         L.mbo_run.argtypes = [C.c_void_p, C.c_int, C.c_uint32]
+        L.mbo_run_red.argtypes = [C.c_void_p, C.c_int, C.c_uint32, C.c_int]
         L.mbo_num_results.argtypes = [C.c_void_p, C.POINTER(C.c_uint32)]
         L.mbo_result_shape.argtypes = [C.c_void_p, C.c_uint32,
                                        C.POINTER(C.c_uint32),
@@ -97,10 +98,17 @@ class OracleRun:
         self._L.mbo_grid(self._h, C.byref(g))
         return g
 
-    def run(self, threads=None, max_steps=0):
+    def run(self, threads=None, max_steps=0, red=0):
+        """solver_cpu_fdtd's loop, or with red > 0 the temporally blocked
+        loop of solver_cpu_fdtd_red with an overlap of `red` steps (the
+        same results bit for bit)."""
         if threads is None:
             threads = os.cpu_count() or 1
-        rc = self._L.mbo_run(self._h, int(threads), int(max_steps))
+        if red:
+            rc = self._L.mbo_run_red(self._h, int(threads), int(max_steps),
+                                     int(red))
+        else:
+            rc = self._L.mbo_run(self._h, int(threads), int(max_steps))
         if rc != 0:
             raise OracleError(self._L.mbo_last_error().decode())
 

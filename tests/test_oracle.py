@@ -263,3 +263,37 @@ def test_grid_derivation_nonzero_length_and_time():
     assert g.num_timesteps == n_t
     assert g.timestep_size == pytest.approx(t_e / (n_t - 1), rel=1e-12)
     assert g.gridpoint_size == pytest.approx(d_x, rel=1e-12)
+
+
+@pytest.mark.parametrize("spec,algo,N", [
+    ({"setup": "sit_2lvl", "kw": dict(num_gridpoints=2000, num_timesteps=500)},
+     "cvr-rodr", 2),
+    ({"setup": "ziolkowski1995", "kw": dict(num_gridpoints=1024,
+                                            endtime=40e-15)}, "cvr-rodr", 2),
+    ({"setup": "ziolkowski1995", "kw": dict(num_gridpoints=1024,
+                                            endtime=40e-15)}, "noop", 0),
+    ({"setup": "lambda_3lvl", "kw": dict(num_gridpoints=600,
+                                         num_timesteps=300)}, "reg-cayley", 3),
+    ({"setup": "random_nlvl", "kw": dict(N=4, num_gridpoints=700,
+                                         num_timesteps=203, e_seed=3e7)},
+     "cvr-rodr", 4),
+])
+@pytest.mark.parametrize("threads", [1, 3])
+def test_blocked_loop_equals_plain_loop(spec, algo, N, threads):
+    """The oracle's restatement of solver_cpu_fdtd_red (thread-private
+    ranges with 8-step overlaps) gives solver_cpu_fdtd's results bit for
+    bit, sources, records and boundaries included, with any step count
+    (not a multiple of the overlap) and any thread count."""
+    from oracle import oracle as O
+    out = []
+    for red in (0, 8):
+        mb.material.clear_library()
+        dev, sce = helpers.build_setup(spec)
+        if spec["setup"] == "ziolkowski1995":
+            sce.add_record(mb.record("h", mb.record.magnetic, 0, 0, 0.0, -1.0))
+        o = O.OracleRun(algo, N, mb.to_pod(dev, sce))
+        o.run(threads=threads, red=red)
+        o.run(threads=threads, max_steps=37, red=red)   # continues
+        out.append([r for r, _ in o.results()])
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
