@@ -260,7 +260,16 @@ int mbg_solver_grid(const mbg_solver* s, mbg_grid* out);
 
 /* Replaces solver_cpu_fdtd::run (solver_cpu_fdtd.tpp:223-338): all
  * num_timesteps steps on the GPU; like the reference, a second call
- * continues from the state the first left. */
+ * continues from the state the first left. Returns MBG_ERR_RUNTIME when a
+ * recorded value was NaN or Inf (the run diverged) or a device wait ran
+ * out; the results stay readable. Device waits are bounded: the
+ * environment variable MBG_WAIT_LIMIT (read when a solver or ensemble is
+ * created) sets how many times a kernel polls before it gives up, where
+ * 0 or unset keeps the kernels' defaults (2^24 polls for a neighbour tile
+ * of the persistent kernel, 2^22 for a tensor-core or bulk-copy
+ * completion). MBG_TEST_STALL_PERSIST=1 exists for tests only: every wait
+ * of the persistent kernel then asks for progress no tile reaches and runs
+ * out. */
 int mbg_solver_run(mbg_solver* s);
 
 /* Results, one per scenario record in record order (solver_cpu_fdtd.tpp:
@@ -299,9 +308,12 @@ int mbg_ensemble_create(
     const mbg_tuning* tuning, /* may be NULL */
     mbg_ensemble** out);
 
-/* Advance every run by up to n_steps time steps (all on the GPU). */
+/* Advance every run by up to n_steps time steps (all on the GPU; the call
+ * returns once the work is queued: mbg_ensemble_status reports device
+ * errors). */
 int mbg_ensemble_advance(mbg_ensemble* e, uint32_t n_steps);
-/* Advance to the end of the longest run. */
+/* Advance to the end of the longest run; MBG_ERR_RUNTIME as for
+ * mbg_solver_run. */
 int mbg_ensemble_run(mbg_ensemble* e);
 /* Time steps done so far and the maximum over runs. */
 int mbg_ensemble_progress(
@@ -352,8 +364,9 @@ int mbg_ensemble_stream_time(mbg_ensemble* e, int begin, double* milliseconds);
 /* Kernels this library launched on the ensemble's stream so far (time-step
  * kernels and the small clock/gather kernels around them). */
 int mbg_ensemble_launches(const mbg_ensemble* e, uint64_t* launches);
-/* Status flags raised on the device (bit 0: non-finite probe value;
- * bit 3: a tensor-core completion wait ran out). */
+/* Status flags raised on the device (bit 0: a recorded value was NaN or
+ * Inf; bit 3: a tensor-core or bulk-copy completion wait ran out; bit 4: a
+ * persistent-kernel wait for neighbour tiles ran out). */
 int mbg_ensemble_status(mbg_ensemble* e, uint32_t* flags);
 /* Checkpoint and resume (no reference counterpart; the reference has no
  * checkpointing). The state is every field, density and record value plus
@@ -393,10 +406,10 @@ int mbg_material_constants(
  * owns, on `stream` (NULL: the legacy default stream); the call returns
  * when it is done. The FP64 workspace is a fixed array of about 160 KB in
  * this library's device memory (enough for 6 levels); larger workspaces
- * are refused with MBG_ERR_INVALID_ARGUMENT. The first call on a device
- * looks up the array's device address; make that call before any stream
- * capture. Every call uses the same array: calls that overlap on the GPU
- * race. With out_device NULL only *len (the block size) is written. */
+ * are refused with MBG_ERR_INVALID_ARGUMENT. Each call looks up the
+ * array's address on the current device and synchronizes `stream` before
+ * it returns. Every call uses the same array: calls that overlap on the
+ * GPU race. With out_device NULL only *len (the block size) is written. */
 int mbg_material_constants_noalloc(
     const char* algo,
     const mbg_material* mat,

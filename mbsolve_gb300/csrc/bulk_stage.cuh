@@ -99,7 +99,8 @@ __device__ __forceinline__ bool load(const kparams<float>& p, uint64_t gt, uint3
     }
     __syncthreads();  // the barrier is initialised before anyone waits on it
     bool ok = false;
-    for (uint32_t i = 0; i < WAIT_LIMIT; i++) {
+    const uint32_t limit = p.wait_limit ? p.wait_limit : WAIT_LIMIT;
+    for (uint32_t i = 0; i < limit; i++) {
         uint32_t done;
         asm volatile(
             "{\n"

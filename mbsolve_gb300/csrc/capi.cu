@@ -31,6 +31,18 @@ int guarded(F&& f)
     }
 }
 
+// Device status after a complete run: a wait that ran out or a recorded
+// NaN/Inf ends the call with MBG_ERR_RUNTIME (the results stay readable).
+void check_status(uint32_t st)
+{
+    if (st & mbg::STATUS_TC_WAIT)
+        throw std::runtime_error("CUDA: a tensor-core or bulk-copy completion wait ran out");
+    if (st & mbg::STATUS_PERSIST_WAIT)
+        throw std::runtime_error("CUDA: a persistent-kernel wait for neighbour tiles ran out");
+    if (st & mbg::STATUS_NONFINITE)
+        throw std::runtime_error("non-finite value (NaN or Inf) recorded: the simulation diverged");
+}
+
 void fill_grid(const mbg::run_setup& r, mbg_grid* g)
 {
     g->num_gridpoints = r.n_x;
@@ -130,10 +142,7 @@ int mbg_solver_run(mbg_solver* s)
         // time index (sources, record rows) starting at 0
         s->eng->restart_clock();
         s->eng->advance(s->eng->steps_total());
-        const uint32_t st = s->eng->status();
-        if (st & mbg::STATUS_TC_WAIT) throw std::runtime_error("CUDA: a tensor-core completion wait ran out");
-        if (st & mbg::STATUS_PERSIST_WAIT)
-            throw std::runtime_error("CUDA: a persistent-kernel wait for neighbour tiles ran out");
+        check_status(s->eng->status());
     });
 }
 
@@ -214,6 +223,7 @@ int mbg_ensemble_run(mbg_ensemble* e)
     return guarded([&] {
         if (!e) throw mbg::invalid_argument("null argument");
         e->eng->advance(e->eng->steps_total());
+        check_status(e->eng->status());
     });
 }
 
@@ -451,7 +461,8 @@ size_t mbg_material_layout(const char* algo, uint32_t N, char* buf, size_t len)
         s << "a=" << L.a << "\nb=" << L.b << "\ncH=" << L.cH << "\ngamma=" << L.gam << "\nhas_qm=" << L.has_qm
           << "\nkH0=" << L.kH0 << "\nkMu=" << L.kMu << "\nW0=" << L.W0 << "\nMn=" << L.Mn << "\ndD1=" << L.dD1
           << "\nd1=" << L.d1 << "\ndD2=" << L.dD2 << "\nd2=" << L.d2 << "\nrho0=" << L.rho0
-          << "\ngP=" << L.gP << "\nstride=" << L.stride;
+          << "\ngP=" << L.gP << "\nstage64=" << L.stage64 << "\nU0=" << L.U0 << "\nWk=" << L.Wk
+          << "\nNP=" << L.NP << "\nB0=" << L.B0 << "\nB0l=" << L.B0l << "\nstride=" << L.stride;
     }
     std::string t = s.str();
     if (buf && len) {

@@ -78,6 +78,8 @@ struct persist_params {
     uint32_t* work;      // work counter, zero at the launch
     uint32_t* prog;      // per tile: levels finished (absolute)
     const int2* nb;      // per tile: left and right neighbour in its run (itself if none)
+    uint32_t wait_limit; // polls of a wait for neighbour tiles (0: the kernel's default)
+    uint32_t stall;      // 0; tests set 1 << 30 so that every wait runs out
 };
 
 // Kernel-side record types beyond MBG_RECORD_*: a coherence record (the

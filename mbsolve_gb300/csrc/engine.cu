@@ -427,7 +427,13 @@ __global__ void init_kernel(
                 }
             } else {
                 const pre::cay_layout L = pre::make_cay_layout(N);
-                for (int v = 0; v < planes; v++) D[(uint64_t) v * plane + g] = qm ? (T) cb[L.rho0 + v] : T(0);
+                const int NN = N * N;
+                for (int v = 0; v < NN; v++) {
+                    const double r0 = qm ? cb[L.rho0 + v] : 0.0;
+                    D[(uint64_t) v * plane + g] = (T) r0;
+                    // FP32: the low word of the float pair
+                    if (planes == 2 * NN) D[(uint64_t) (NN + v) * plane + g] = (T) (r0 - (double) (T) r0);
+                }
             }
         }
     }
@@ -577,10 +583,15 @@ public:
     engine_t(const solver_kind& k, std::vector<run_setup>&& runs, const mbg_tuning* t)
       : kind_(k), runs_(std::move(runs))
     {
-        // FP32 coherence vectors are float pairs: V high then V low planes
+        // FP32 density states are float pairs: the high planes, then the
+        // low planes
         planes_ = (k.algo == ALGO_CVR) ? (k.N * k.N - 1) * (DF ? 2 : 1)
-            : (k.algo == ALGO_CAYLEY)  ? k.N * k.N
+            : (k.algo == ALGO_CAYLEY)  ? k.N * k.N * (DF ? 2 : 1)
                                        : 0;
+        // bound of the kernels' device-side waits (polls), and the test
+        // switch that makes every persistent-kernel wait run out
+        if (const char* w = std::getenv("MBG_WAIT_LIMIT")) wait_limit_ = (uint32_t) std::strtoul(w, nullptr, 10);
+        if (const char* w = std::getenv("MBG_TEST_STALL_PERSIST")) stall_ = (w[0] == '1') ? (1u << 30) : 0u;
         MBG_CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
         setup();
         choose_tuning(t);
@@ -676,7 +687,49 @@ public:
         char magic[8];
         uint32_t version, real_bytes, algo, levels;
         uint64_t n_total, planes, scratch, runs, nt_max, steps_done;
+        uint64_t digest;  // of the run descriptions (describe_digest)
     };
+
+    // FNV-1a (64 bit) over the descriptions that determine how a state
+    // evolves: grid and step, boundary, materials (the precompute's FP64
+    // inputs), regions, sources (with their tables) and records. Initial
+    // conditions are left out: a checkpoint replaces the state they set.
+    static uint64_t describe_digest(const std::vector<run_setup>& runs)
+    {
+        uint64_t h = 1469598103934665603ull;
+        auto bytes = [&](const void* p, size_t n) {
+            const unsigned char* c = static_cast<const unsigned char*>(p);
+            for (size_t i = 0; i < n; i++) {
+                h ^= c[i];
+                h *= 1099511628211ull;
+            }
+        };
+        auto num = [&](auto v) { bytes(&v, sizeof(v)); };
+        num((uint64_t) runs.size());
+        for (const run_setup& r : runs) {
+            num(r.n_x), num(r.n_t), num(r.dx), num(r.dt), num(r.endtime);
+            num(r.k_left), num(r.k_right);
+            num((uint64_t) r.mats.size());
+            for (const pre::mat_in& m : r.mats) {
+                num(m.N), num(m.relax_kind), num(m.eps_r), num(m.mu_r), num(m.overlap), num(m.losses);
+                num(m.carrier_density), num(m.dt), num(m.dx);
+                bytes(m.h_re, sizeof(m.h_re)), bytes(m.h_im, sizeof(m.h_im));
+                bytes(m.mu_re, sizeof(m.mu_re)), bytes(m.mu_im, sizeof(m.mu_im));
+                bytes(m.S, sizeof(m.S)), bytes(m.deph, sizeof(m.deph));
+            }
+            for (const auto& g : r.regions) num(g.mat), num(g.x0), num(g.x1);
+            for (const auto& s : r.sources) {
+                num(s.type), num(s.shape), num(s.x_idx), num(s.on_grid), num(s.ampl), num(s.freq);
+                num(s.phase), num(s.beta_or_tau), num(s.phase_sin);
+                if (!s.table.empty()) bytes(s.table.data(), s.table.size() * sizeof(double));
+            }
+            for (const auto& c : r.records) {
+                num(c.d.type), num(c.d.row_idx), num(c.d.col_idx), num(c.d.pos), num(c.d.cols);
+                num(c.d.rows), num(c.d.ratio), num(c.is_complex), num(c.coherence);
+            }
+        }
+        return h;
+    }
 
     uint64_t state_bytes() const override
     {
@@ -688,7 +741,7 @@ public:
     {
         state_header h{};
         std::memcpy(h.magic, "MBGSTATE", 8);
-        h.version = 1;
+        h.version = 2;
         h.real_bytes = sizeof(T);
         h.algo = (uint32_t) kind_.algo;
         h.levels = (uint32_t) kind_.N;
@@ -698,6 +751,7 @@ public:
         h.runs = runs_.size();
         h.nt_max = nt_max_;
         h.steps_done = steps_done_;
+        h.digest = digest_;
         return h;
     }
 
@@ -739,6 +793,9 @@ public:
         if (h.real_bytes != m.real_bytes || h.algo != m.algo || h.levels != m.levels || h.n_total != m.n_total ||
             h.planes != m.planes || h.scratch != m.scratch || h.runs != m.runs || h.nt_max != m.nt_max)
             throw invalid_argument("checkpoint does not match this ensemble");
+        if (h.digest != m.digest)
+            throw invalid_argument(
+                "checkpoint belongs to an ensemble of other descriptions (grid, materials, sources or records)");
         if (bytes < state_bytes()) throw invalid_argument("checkpoint truncated");
         if (h.steps_done > nt_max_) throw invalid_argument("checkpoint step out of range");
         const char* i = static_cast<const char*>(host) + sizeof(h);
@@ -828,6 +885,9 @@ private:
     dbuf<int2> nb_;
     dbuf<uint32_t> prog_, work_;
     uint32_t pbase_ = 0;
+    uint64_t digest_ = 0;  // describe_digest(runs_), for checkpoints
+    uint32_t wait_limit_ = 0;  // MBG_WAIT_LIMIT (0: the kernels' defaults)
+    uint32_t stall_ = 0;       // MBG_TEST_STALL_PERSIST
     persist_fn<T> pfn_ = nullptr;
     int persist_ = 0;
     dbuf<unsigned long long> step_, step_zero_;
@@ -870,6 +930,7 @@ private:
 
     void setup()
     {
+        digest_ = describe_digest(runs_);
         const uint32_t nr = (uint32_t) runs_.size();
         if (nr == 0) throw invalid_argument("no runs");
         // packed ragged layout: runs back to back, 8-point aligned
@@ -920,7 +981,9 @@ private:
             mstride_ = pre::make_cvr_layout(N).stride;
             mstage_ = pre::make_cvr_layout(N).stage;
         } else if (kind_.algo == ALGO_CAYLEY) {
-            mstride_ = mstage_ = pre::make_cay_layout(N).stride;
+            // the FP64 kernels read only the leading part of the block
+            mstride_ = pre::make_cay_layout(N).stride;
+            mstage_ = DF ? mstride_ : pre::make_cay_layout(N).stage64;
         } else {
             mstride_ = pre::make_cvr_layout(0).stride;
             mstage_ = pre::make_cvr_layout(0).stage;
@@ -1239,6 +1302,7 @@ private:
         p.halo = (uint32_t) align_halo(tune_.depth);
         p.record = record ? 1 : 0;
         p.status = status_.p;
+        p.wait_limit = wait_limit_;
         return p;
     }
 
@@ -1297,6 +1361,8 @@ private:
         q.work = work_.p;
         q.prog = prog_.p;
         q.nb = nb_.p;
+        q.wait_limit = wait_limit_;
+        q.stall = stall_;
         // level k reads buffer cur_ ^ (k & 1): the kernel flips odd levels
         kparams<T> p = params(cur_, 0, nsub, true, step_.p);
         pfn_(p, q, smem(), stream_);

@@ -68,12 +68,13 @@ struct kparams {
     uint32_t halo;
     int record;           // 0 while autotuning
     uint32_t* status;
+    uint32_t wait_limit;  // polls of a bounded device wait (0: the kernel's default)
 };
 
 // ------------------------------------------------------------ helpers
 
-// sin(x) and 1 - cos(x). For |x| < 1/4 by their Taylor series (enough
-// terms for the type's precision: truncation below 1e-16 relative in
+// sin(x) and 1 - cos(x). For small |x| by their Taylor series (enough
+// terms for the type's precision: truncation below 1e-12 relative in
 // float, 1e-30 in double); beyond that by the library sincos.
 template<typename T>
 __device__ __forceinline__ void rot_coeffs(T x, T& s, T& s2);
@@ -81,20 +82,20 @@ __device__ __forceinline__ void rot_coeffs(T x, T& s, T& s2);
 template<>
 __device__ __forceinline__ void rot_coeffs<float>(float x, float& s, float& s2)
 {
-    if (fabsf(x) < 0.25f) {
-        float x2 = x * x;
-        // sin x = x (1 - x^2/(2*3) (1 - x^2/(4*5) (1 - x^2/(6*7) (1 - x^2/(8*9)))))
-        float t = 1.0f - x2 * (1.0f / 72.0f);
-        t = 1.0f - x2 * (1.0f / 42.0f) * t;
-        t = 1.0f - x2 * (1.0f / 20.0f) * t;
-        t = 1.0f - x2 * (1.0f / 6.0f) * t;
-        s = x * t;
-        // 1 - cos x = x^2/2 (1 - x^2/(3*4) (1 - x^2/(5*6) (1 - x^2/(7*8) (1 - x^2/(9*10)))))
-        float u = 1.0f - x2 * (1.0f / 90.0f);
-        u = 1.0f - x2 * (1.0f / 56.0f) * u;
-        u = 1.0f - x2 * (1.0f / 30.0f) * u;
-        u = 1.0f - x2 * (1.0f / 12.0f) * u;
-        s2 = 0.5f * x2 * u;
+    // |x| < 1/16 (the field rotation per step is far smaller in every
+    // workload here: ~1e-3): the series to x^7 and x^8, Horner in x^2;
+    // the first omitted terms are below 1e-14 of the result
+    if (fabsf(x) < 0.0625f) {
+        const float x2 = x * x;
+        // sin x = x (1 - x^2/3! + x^4/5! - x^6/7!)
+        float t = fmaf(x2, -1.0f / 5040.0f, 1.0f / 120.0f);
+        t = fmaf(x2, t, -1.0f / 6.0f);
+        s = fmaf(x * x2, t, x);
+        // 1 - cos x = x^2/2! - x^4/4! + x^6/6! - x^8/8!
+        float u = fmaf(x2, 1.0f / 40320.0f, -1.0f / 720.0f);
+        u = fmaf(x2, u, 1.0f / 24.0f);
+        u = fmaf(x2, -u, 0.5f);
+        s2 = x2 * u;
     } else {
         float c;
         sincosf(x, &s, &c);
@@ -416,35 +417,43 @@ struct cvr_coef_reg {
     __device__ __forceinline__ const cvr_coef_reg& pass() const { return *this; }  // stays in registers
 };
 
-// The same step in FP32 with v = uh + ul: the rotation and the correction
-// are computed in FP32 from the high words and accumulated error-free; the
-// low words take the rounding errors and the Bdl contribution; one
-// renormalisation per step.
+// The same step in FP32 with v = uh + ul: the rotation increment d and
+// the correction s = k + Bd r, r = fl(uh + d) the rotated high words, are
+// computed in FP32 and their sum d + s is accumulated error-free (one
+// TwoSum per entry; rounding d + s first costs ~3e-8 of an increment of
+// ~1e-2, far below the low words' resolution); the low words take the
+// rounding errors and the Bdl contribution; one renormalisation per step.
 template<int V, class CF>
 __device__ __forceinline__ void cvr_update_df(float (&uh)[V], float (&ul)[V], float e, float& pout, const CF& cf)
 {
     const auto c = cf.pass();
+    float d[V], r[V];
+    static_for<0, V>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        d[i] = 0.0f;
+        r[i] = uh[i];
+    });
     static_for<0, V / 2>([&](auto K) {
         constexpr int k = decltype(K)::value;
         float sn, s2;
         rot_coeffs<float>(c.th(k) * e, sn, s2);
         const float a = uh[2 * k], b = uh[2 * k + 1];
-        const float da = -fmaf(s2, a, sn * b);
-        const float db = fmaf(sn, a, -s2 * b);
-        df_acc(uh[2 * k], ul[2 * k], da, 0.0f);
-        df_acc(uh[2 * k + 1], ul[2 * k + 1], db, 0.0f);
+        d[2 * k] = -fmaf(s2, a, sn * b);
+        d[2 * k + 1] = fmaf(sn, a, -s2 * b);
+        r[2 * k] = a + d[2 * k];
+        r[2 * k + 1] = b + d[2 * k + 1];
     });
     float s[V], sl[V];
     static_for<0, V>([&](auto I) {
         constexpr int i = decltype(I)::value;
         s[i] = c.k(i);
         sl[i] = 0.0f;
-        row_dot<true, i>(c, uh, s[i], sl[i]);
+        row_dot<true, i>(c, r, s[i], sl[i]);
     });
     float pp = c.p0();
     static_for<0, V>([&](auto I) {
         constexpr int i = decltype(I)::value;
-        df_acc(uh[i], ul[i], s[i], sl[i]);
+        df_acc(uh[i], ul[i], d[i] + s[i], sl[i]);
         df_renorm(uh[i], ul[i]);
         pp = fmaf(c.g(i), uh[i], fmaf(c.g(i), ul[i], pp));
     });
@@ -772,6 +781,196 @@ __device__ __forceinline__ void cayley_update(T (&rho)[N * N], T e, T& pout, con
     T acc = T(0);
 #pragma unroll
     for (int i = 0; i < N * N; i++) acc = fma(cf[L.gP + i], rho[i], acc);
+    pout = acc;
+}
+
+// The same step in FP32 on rho = rh + rl (float pairs), split as in
+// cay_layout: rho <- rho + B0 rho + D(E(D rho)). The field-free part B0 rho
+// uses B0 and its low part B0l (error-free accumulation into the pair);
+// the field-dependent correction E is computed in FP32 from the high words:
+//   s = D(rh);  A(e) Y = W (LU without pivoting: A's Hermitian part is I);
+//   dU = 2 i e Y;  Z = dU s;  E = Z (U0 + dU)^H + U0 Z^H.
+// One renormalisation of the pairs per step; P = gP . rho.
+template<int N>
+__device__ __forceinline__ void cayley_update_df(float (&rh)[N * N], float (&rl)[N * N], float e, float& pout, const float* cf)
+{
+    typedef cpx_f cx;
+    constexpr int NN = N * N;
+    const pre::cay_layout L = pre::make_cay_layout(N);
+    // s = D(rh), packed like rho (entry (l, k) through sget)
+    float sp[NN];
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        float v = rh[i];
+#pragma unroll
+        for (int j = 0; j < N; j++) v = fmaf(cf[L.dD1 + i * N + j], rh[j], v);
+        sp[i] = v;
+    }
+#pragma unroll
+    for (int q = 0; q < (NN - N) / 2; q++) {
+        const float dd = cf[L.dD2 + q];
+        sp[N + 2 * q] = fmaf(dd, rh[N + 2 * q], rh[N + 2 * q]);
+        sp[N + 2 * q + 1] = fmaf(dd, rh[N + 2 * q + 1], rh[N + 2 * q + 1]);
+    }
+    auto sget = [&](int l, int k) -> cx {
+        cx v;
+        if (l == k) {
+            v.re = sp[l];
+            v.im = 0.0f;
+        } else {
+            const int a = l < k ? l : k, b = l < k ? k : l;
+            const int q = b * (b - 1) / 2 + a;
+            v.re = sp[N + 2 * q];
+            v.im = l < k ? sp[N + 2 * q + 1] : -sp[N + 2 * q + 1];
+        }
+        return v;
+    };
+    // A = I + i (kappa H0 - e kappa mu); Y = W
+    cx A[N][N], Y[N][N];
+#pragma unroll
+    for (int j = 0; j < N; j++)
+#pragma unroll
+        for (int k = 0; k < N; k++) {
+            float kr, ki;
+            if (j == k) {
+                kr = fmaf(-e, cf[L.kMu + j], cf[L.kH0 + j]);
+                ki = 0.0f;
+            } else {
+                const int a = j < k ? j : k, b = j < k ? k : j;
+                const int q = b * (b - 1) / 2 + a;
+                kr = fmaf(-e, cf[L.kMu + N + 2 * q], cf[L.kH0 + N + 2 * q]);
+                ki = fmaf(-e, cf[L.kMu + N + 2 * q + 1], cf[L.kH0 + N + 2 * q + 1]);
+                if (j > k) ki = -ki;
+            }
+            A[j][k].re = (j == k ? 1.0f : 0.0f) - ki;
+            A[j][k].im = kr;
+            Y[j][k].re = cf[L.Wk + j * N + k];
+            Y[j][k].im = cf[L.Wk + NN + j * N + k];
+        }
+    cx pinv[N];
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        const float rden = 1.0f / (A[k][k].re * A[k][k].re + A[k][k].im * A[k][k].im);
+        cx inv;
+        inv.re = A[k][k].re * rden;
+        inv.im = -A[k][k].im * rden;
+        pinv[k] = inv;
+#pragma unroll
+        for (int i = k + 1; i < N; i++) {
+            cx f;
+            f.re = A[i][k].re * inv.re - A[i][k].im * inv.im;
+            f.im = A[i][k].re * inv.im + A[i][k].im * inv.re;
+#pragma unroll
+            for (int j = k + 1; j < N; j++) {
+                A[i][j].re -= f.re * A[k][j].re - f.im * A[k][j].im;
+                A[i][j].im -= f.re * A[k][j].im + f.im * A[k][j].re;
+            }
+#pragma unroll
+            for (int j = 0; j < N; j++) {
+                Y[i][j].re -= f.re * Y[k][j].re - f.im * Y[k][j].im;
+                Y[i][j].im -= f.re * Y[k][j].im + f.im * Y[k][j].re;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = N - 1; k >= 0; k--) {
+        const cx inv = pinv[k];
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            cx v = Y[k][j];
+#pragma unroll
+            for (int i = k + 1; i < N; i++) {
+                v.re -= A[k][i].re * Y[i][j].re - A[k][i].im * Y[i][j].im;
+                v.im -= A[k][i].re * Y[i][j].im + A[k][i].im * Y[i][j].re;
+            }
+            Y[k][j].re = v.re * inv.re - v.im * inv.im;
+            Y[k][j].im = v.re * inv.im + v.im * inv.re;
+        }
+    }
+    // dU = 2 i e Y (in Y); Z = dU s (in A)
+    const float e2 = 2.0f * e;
+#pragma unroll
+    for (int j = 0; j < N; j++)
+#pragma unroll
+        for (int k = 0; k < N; k++) {
+            const float yr = Y[j][k].re;
+            Y[j][k].re = -e2 * Y[j][k].im;
+            Y[j][k].im = e2 * yr;
+        }
+#pragma unroll
+    for (int j = 0; j < N; j++)
+#pragma unroll
+        for (int k = 0; k < N; k++) {
+            float zr = 0.0f, zi = 0.0f;
+#pragma unroll
+            for (int l = 0; l < N; l++) {
+                const cx s = sget(l, k);
+                zr = fmaf(Y[j][l].re, s.re, fmaf(-Y[j][l].im, s.im, zr));
+                zi = fmaf(Y[j][l].re, s.im, fmaf(Y[j][l].im, s.re, zi));
+            }
+            A[j][k].re = zr;
+            A[j][k].im = zi;
+        }
+    // E (packed) = Z (U0 + dU)^H + U0 Z^H
+    float ev[NN];
+#pragma unroll
+    for (int k = 0; k < N; k++)
+#pragma unroll
+        for (int j = 0; j <= k; j++) {
+            float er = 0.0f, ei = 0.0f;
+#pragma unroll
+            for (int l = 0; l < N; l++) {
+                const float u0r = cf[L.U0 + k * N + l], u0i = cf[L.U0 + NN + k * N + l];
+                const float u2r = u0r + Y[k][l].re, u2i = u0i + Y[k][l].im;
+                // Z_jl conj(U2_kl)
+                er = fmaf(A[j][l].re, u2r, fmaf(A[j][l].im, u2i, er));
+                ei = fmaf(A[j][l].im, u2r, fmaf(-A[j][l].re, u2i, ei));
+                // U0_jl conj(Z_kl)
+                const float v0r = cf[L.U0 + j * N + l], v0i = cf[L.U0 + NN + j * N + l];
+                er = fmaf(v0r, A[k][l].re, fmaf(v0i, A[k][l].im, er));
+                ei = fmaf(v0i, A[k][l].re, fmaf(-v0r, A[k][l].im, ei));
+            }
+            if (j == k) {
+                ev[j] = er;
+            } else {
+                const int q = k * (k - 1) / 2 + j;
+                ev[N + 2 * q] = er;
+                ev[N + 2 * q + 1] = ei;
+            }
+        }
+    // increments: D(E) + B0 rh (high part), B0l rh (low part)
+    float inc[NN], incl[NN];
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        float v = ev[i];
+#pragma unroll
+        for (int j = 0; j < N; j++) v = fmaf(cf[L.dD1 + i * N + j], ev[j], v);
+        inc[i] = v;
+    }
+#pragma unroll
+    for (int q = 0; q < (NN - N) / 2; q++) {
+        const float dd = cf[L.dD2 + q];
+        inc[N + 2 * q] = fmaf(dd, ev[N + 2 * q], ev[N + 2 * q]);
+        inc[N + 2 * q + 1] = fmaf(dd, ev[N + 2 * q + 1], ev[N + 2 * q + 1]);
+    }
+#pragma unroll
+    for (int v = 0; v < NN; v++) {
+        float a = inc[v], b = 0.0f;
+#pragma unroll
+        for (int w = 0; w < NN; w++) {
+            a = fmaf(cf[L.B0 + v * L.NP + w], rh[w], a);
+            b = fmaf(cf[L.B0l + v * L.NP + w], rh[w], b);
+        }
+        inc[v] = a;
+        incl[v] = b;
+    }
+    float acc = 0.0f;
+#pragma unroll
+    for (int v = 0; v < NN; v++) {
+        df_acc(rh[v], rl[v], inc[v], incl[v]);
+        df_renorm(rh[v], rl[v]);
+        acc = fmaf(cf[L.gP + v], rh[v], fmaf(cf[L.gP + v], rl[v], acc));
+    }
     pout = acc;
 }
 

@@ -182,10 +182,30 @@ MBG_HD cvr_layout make_cvr_layout(int N)
 // Constant block of one material for the Cayley kernels. Hermitian
 // operators are packed as N real diagonal entries followed by the upper
 // triangle in column-major order as (re, im) pairs: N^2 reals.
+//
+// The FP64 kernels follow the reference's step (reg_cayley.hpp:228-257)
+// with the entries up to `stage64`. The FP32 kernels split the step into
+// its field-free part and a field-dependent correction. With
+// A(e) = I + i kappa (H0 - e mu), U2(e) = A(e)^-1 (I - i kappa (H0 - e mu))
+// = 2 A(e)^-1 - I and D the dissipation half step,
+//   rho <- D Ad(U2(e)) D rho = T0 rho + D(E(D rho)),
+//   T0 = D Ad(U0) D (U0 = U2(0)),
+//   E(s) = Ad(U2) s - Ad(U0) s = Z U2^H + U0 Z^H,  Z = dU s,
+//   dU = U2(e) - U0 = 2 i e A(e)^-1 W,  W = kappa mu A(0)^-1.
+// T0 - I (B0, a real N^2 x N^2 matrix on packed coordinates) is computed
+// here in FP64 and stored as a float pair (B0 and B0l = B0 - fl32(B0)), so
+// the free evolution that dominates every step carries no FP32 rounding
+// (in FP32 it shifts the transition frequencies by ~1e-7 relative, which
+// over 1e5 steps is a phase error far above 1e-5); dU is proportional to e
+// and only needs FP32's relative accuracy. Full complex matrices are
+// stored row-major as N^2 real parts then N^2 imaginary parts; B0 rows are
+// padded to a multiple of 4 entries.
 struct cay_layout {
     int N, P;
     int a, b, cH, gam, has_qm;
-    int kH0, kMu, W0, Mn, dD1, d1, dD2, d2, rho0, gP, stride;
+    int kH0, kMu, W0, Mn, dD1, d1, dD2, d2, rho0, gP;
+    int stage64;  // leading part the FP64 kernels use and stage
+    int U0, Wk, NP, B0, B0l, stride;
 };
 
 MBG_HD cay_layout make_cay_layout(int N)
@@ -219,6 +239,18 @@ MBG_HD cay_layout make_cay_layout(int N)
     o += N * N;
     L.gP = o;  // P = gP . (packed density matrix)
     o += N * N;
+    o = (o + 3) & ~3;
+    L.stage64 = o;
+    L.U0 = o;
+    o += 2 * N * N;
+    L.Wk = o;
+    o += 2 * N * N;
+    o = (o + 3) & ~3;
+    L.NP = (N * N + 3) & ~3;
+    L.B0 = o;
+    o += N * N * L.NP;
+    L.B0l = o;
+    o += N * N * L.NP;
     L.stride = (o + 3) & ~3;
     return L;
 }
@@ -940,7 +972,7 @@ MBG_HD int cvr_precompute(const mat_in& m, int Nsolver, double* ws, double* out)
 }
 
 // Workspace doubles needed by cay_precompute.
-MBG_HD size_t cay_workspace(int N) { return (size_t) N * N * 5 + 16; }
+MBG_HD size_t cay_workspace(int N) { return (size_t) N * N * 18 + 16; }
 
 MBG_HD void pack_hermitian(const double* re, const double* im, int N, double s, double* out)
 {
@@ -1013,6 +1045,170 @@ MBG_HD void cay_polarisation_weights(const cay_layout& L, double* out)
         }
 }
 
+// Solves A X = B for n x n complex A and n x m complex B (row-major; A and B
+// are overwritten, X is left in B) by Gaussian elimination with partial
+// pivoting on the modulus.
+MBG_HD void csolve(cd* A, cd* B, int n, int m)
+{
+    for (int k = 0; k < n; k++) {
+        int p = k;
+        double best = A[k * n + k].re * A[k * n + k].re + A[k * n + k].im * A[k * n + k].im;
+        for (int i = k + 1; i < n; i++) {
+            const double v = A[i * n + k].re * A[i * n + k].re + A[i * n + k].im * A[i * n + k].im;
+            if (v > best) {
+                best = v;
+                p = i;
+            }
+        }
+        if (p != k) {
+            for (int j = 0; j < n; j++) {
+                const cd t = A[k * n + j];
+                A[k * n + j] = A[p * n + j];
+                A[p * n + j] = t;
+            }
+            for (int j = 0; j < m; j++) {
+                const cd t = B[k * m + j];
+                B[k * m + j] = B[p * m + j];
+                B[p * m + j] = t;
+            }
+        }
+        const cd piv = A[k * n + k];
+        const double den = piv.re * piv.re + piv.im * piv.im;
+        const cd inv = cmake(piv.re / den, -piv.im / den);
+        for (int i = k + 1; i < n; i++) {
+            const cd f = cmul(A[i * n + k], inv);
+            for (int j = k; j < n; j++) A[i * n + j] = csub(A[i * n + j], cmul(f, A[k * n + j]));
+            for (int j = 0; j < m; j++) B[i * m + j] = csub(B[i * m + j], cmul(f, B[k * m + j]));
+        }
+    }
+    for (int k = n - 1; k >= 0; k--) {
+        const cd piv = A[k * n + k];
+        const double den = piv.re * piv.re + piv.im * piv.im;
+        const cd inv = cmake(piv.re / den, -piv.im / den);
+        for (int j = 0; j < m; j++) {
+            cd s = B[k * m + j];
+            for (int i = k + 1; i < n; i++) s = csub(s, cmul(A[k * n + i], B[i * m + j]));
+            B[k * m + j] = cmul(s, inv);
+        }
+    }
+}
+
+// Full Hermitian matrix (n x n, row-major) from its packed form, and back.
+MBG_HD void herm_unpack(const double* p, int N, cd* F)
+{
+    for (int j = 0; j < N; j++)
+        for (int k = 0; k < N; k++) herm_at(p, N, j, k, F[j * N + k].re, F[j * N + k].im);
+}
+MBG_HD void herm_pack(const cd* F, int N, double* p)
+{
+    for (int i = 0; i < N; i++) p[i] = F[i * N + i].re;
+    for (int k = 1; k < N; k++)
+        for (int j = 0; j < k; j++) {
+            const int q = upper_index(j, k);
+            p[N + 2 * q] = F[j * N + k].re;
+            p[N + 2 * q + 1] = F[j * N + k].im;
+        }
+}
+
+// (D - I) r for the dissipation half step D on a packed density matrix:
+// populations by D1 - I, the coherence of pair q by D2_q - 1.
+MBG_HD void cay_dissipation_increment(const cay_layout& L, const double* out, const double* r, double* d)
+{
+    const int N = L.N;
+    for (int i = 0; i < N; i++) {
+        double s = 0.0;
+        for (int j = 0; j < N; j++) s += out[L.dD1 + i * N + j] * r[j];
+        d[i] = s;
+    }
+    for (int q = 0; q < L.P; q++) {
+        d[N + 2 * q] = out[L.dD2 + q] * r[N + 2 * q];
+        d[N + 2 * q + 1] = out[L.dD2 + q] * r[N + 2 * q + 1];
+    }
+}
+
+// The field-free part of the FP32 Cayley step (see cay_layout): U0, W and
+// B0 = D Ad(U0) D - I from kH0, kMu, dD1 and dD2, all in FP64. B0's
+// columns are formed as sums of small increments (never as T0 e - e), so
+// its entries keep their relative accuracy however small the rates.
+// ws: 17 N^2 doubles.
+MBG_HD void cay_free_step(const cay_layout& L, double* ws, double* out)
+{
+    const int N = L.N, NN = N * N;
+    cd* A = reinterpret_cast<cd*>(ws);  // NN
+    cd* B = A + NN;                      // N x 2N: [Y | A0^-1]
+    cd* X = B + 2 * NN;                  // X0 = U0 - I
+    cd* K = X + NN;                      // K1, then scratch
+    cd* S = K + NN;                      // sigma (full)
+    cd* G = S + NN;                      // X0 sigma
+    double* r = reinterpret_cast<double*>(G + NN);  // NN packed
+    double* t = r + NN;
+    double* d = t + NN;
+    // A0 = I + i K0; solve A0 [Y | Ai] = [K0 | I]
+    for (int j = 0; j < N; j++)
+        for (int k = 0; k < N; k++) {
+            double kr, ki;
+            herm_at(out + L.kH0, N, j, k, kr, ki);
+            A[j * N + k] = cmake((j == k ? 1.0 : 0.0) - ki, kr);
+            B[j * 2 * N + k] = cmake(kr, ki);
+            B[j * 2 * N + N + k] = cmake(j == k ? 1.0 : 0.0, 0.0);
+        }
+    csolve(A, B, N, 2 * N);
+    // X0 = -2i Y; U0 = I + X0
+    for (int j = 0; j < N; j++)
+        for (int k = 0; k < N; k++) {
+            const cd y = B[j * 2 * N + k];
+            X[j * N + k] = cmake(2.0 * y.im, -2.0 * y.re);
+            out[L.U0 + j * N + k] = (j == k ? 1.0 : 0.0) + X[j * N + k].re;
+            out[L.U0 + NN + j * N + k] = X[j * N + k].im;
+        }
+    // W = K1 A0^-1
+    for (int j = 0; j < N; j++)
+        for (int k = 0; k < N; k++) {
+            double kr, ki;
+            herm_at(out + L.kMu, N, j, k, kr, ki);
+            K[j * N + k] = cmake(kr, ki);
+        }
+    for (int j = 0; j < N; j++)
+        for (int k = 0; k < N; k++) {
+            cd s = cmake(0.0, 0.0);
+            for (int l = 0; l < N; l++) s = cadd(s, cmul(K[j * N + l], B[l * 2 * N + N + k]));
+            out[L.Wk + j * N + k] = s.re;
+            out[L.Wk + NN + j * N + k] = s.im;
+        }
+    // columns of B0: e_v -> (D - I) e_v + pack(Ad(U0) s - s) + (D - I) tau,
+    // s = D e_v, tau = Ad(U0) s
+    for (int v = 0; v < NN; v++) {
+        for (int i = 0; i < NN; i++) r[i] = (i == v) ? 1.0 : 0.0;
+        cay_dissipation_increment(L, out, r, d);  // (D - I) e_v
+        for (int i = 0; i < NN; i++) t[i] = r[i] + d[i];
+        herm_unpack(t, N, S);
+        // Ad(U0) s - s = X0 s + (X0 s)^H + X0 s X0^H
+        for (int j = 0; j < N; j++)
+            for (int k = 0; k < N; k++) {
+                cd g = cmake(0.0, 0.0);
+                for (int l = 0; l < N; l++) g = cadd(g, cmul(X[j * N + l], S[l * N + k]));
+                G[j * N + k] = g;
+            }
+        for (int j = 0; j < N; j++)
+            for (int k = 0; k < N; k++) {
+                cd h = cadd(G[j * N + k], cconj(G[k * N + j]));
+                for (int l = 0; l < N; l++) h = cadd(h, cmul(G[j * N + l], cconj(X[k * N + l])));
+                K[j * N + k] = h;
+            }
+        herm_pack(K, N, r);  // Ad(U0) s - s, packed
+        for (int i = 0; i < NN; i++) {
+            d[i] += r[i];       // column so far: (D - I) e_v + (Ad(U0) s - s)
+            t[i] += r[i];       // tau = s + (Ad(U0) s - s)
+        }
+        cay_dissipation_increment(L, out, t, r);  // (D - I) tau
+        for (int i = 0; i < NN; i++) {
+            const double b = d[i] + r[i];
+            out[L.B0 + i * L.NP + v] = b;
+            out[L.B0l + i * L.NP + v] = b - (double) (float) b;
+        }
+    }
+}
+
 // Cayley constants of one material (cay_layout of `Nsolver` levels).
 // Returns 0, 1 on a level-count mismatch, 3 for a relaxation superoperator
 // that is not of Lindblad form (reg_cayley.hpp:146-155).
@@ -1055,6 +1251,7 @@ MBG_HD int cay_precompute(const mat_in& m, int Nsolver, double* ws, double* out)
         out[L.rho0 + N + 2 * p + 1] = m.rho_off_im[p];
     }
     cay_polarisation_weights(L, out);
+    cay_free_step(L, ws, out);
     return 0;
 }
 

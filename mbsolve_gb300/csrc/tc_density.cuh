@@ -86,6 +86,7 @@ struct ctx {
     uint32_t tmem;
     uint32_t mbar;
     uint32_t phase;
+    uint32_t wait_limit;  // polls of a completion wait
 };
 
 __device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc)
@@ -99,9 +100,9 @@ __device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uin
         "l"(a), "l"(b), "r"(id), "r"(acc));
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint32_t limit)
 {
-    for (uint32_t i = 0; i < WAIT_LIMIT; i++) {
+    for (uint32_t i = 0; i < limit; i++) {
         uint32_t ok;
         asm volatile(
             "{\n"
@@ -226,7 +227,7 @@ __device__ __forceinline__ bool product(ctx& c)
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(c.mbar)
                      : "memory");
     }
-    const bool ok = mbar_wait(c.mbar, c.phase);
+    const bool ok = mbar_wait(c.mbar, c.phase, c.wait_limit);
     c.phase ^= 1u;
     fence_after();
     // the same answer in every thread, so that a time-out ends the tile in

@@ -259,6 +259,8 @@ __device__ __forceinline__ bool tile_steps(
                         else
                             cvr_update<T, D>(R[j], e, P[j], cf);
                     }
+                } else if constexpr (DF) {
+                    cayley_update_df<LEV>(R[j], Rl[j], e, P[j], cb);
                 } else {
                     cayley_update<T, LEV>(R[j], e, P[j], cb);
                 }
@@ -287,7 +289,7 @@ __device__ __forceinline__ bool tile_steps(
                         case 0: v = ev; break;
                         case 1: v = P[j]; break;
                         case 2: v = hv; break;
-                        case 4: v = R[j][1] - R[j][0]; break;
+                        case 4: v = DF ? (R[j][1] - R[j][0]) + (Rl[j][1] - Rl[j][0]) : R[j][1] - R[j][0]; break;
                         default: {
                             // populations (3) and coherence parts (REC_COH_*):
                             // an entry of the packed matrix (diagonal, then
@@ -300,7 +302,7 @@ __device__ __forceinline__ bool tile_steps(
                                                             (rc.type == REC_COH_IM ? 1 : 0);
 #pragma unroll
                             for (int q = 0; q < LEV * LEV; q++)
-                                if (idx == (uint32_t) q) v = R[j][q];
+                                if (idx == (uint32_t) q) v = DF ? R[j][q] + Rl[j][q] : R[j][q];
                             if (rc.type == REC_COH_IM && rc.row_idx > rc.col_idx) v = -v;
                             break;
                         }
@@ -387,7 +389,7 @@ __device__ __forceinline__ void step_body(const kparams<T>& p, uint32_t tile, ui
     constexpr int D = density_len<ALGO, LEV>::value;
     constexpr int DD = D > 0 ? D : 1;
     constexpr int NW = NT / 32;
-    constexpr bool DFD = DF && ALGO == 1;
+    constexpr bool DFD = DF && ALGO != 0;  // FP32 density state as float pairs
     __shared__ T sh_a[NW], sh_al[NW], sh_b[NW], sh_bl[NW];
     __shared__ tile_lists tl;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -555,6 +557,7 @@ __device__ __forceinline__ void step_body(const kparams<T>& p, uint32_t tile, ui
         tcc.tmem = res.tmem;
         tcc.mbar = res.mbar;
         tcc.phase = *res.phase;
+        tcc.wait_limit = p.wait_limit ? p.wait_limit : tc::WAIT_LIMIT;
         if (uniform) tc::stage_b<D>(tcc, p.mc + (uint64_t) td.uniform_mat * p.mstride);
     }
 
@@ -577,7 +580,8 @@ __device__ __forceinline__ void step_body(const kparams<T>& p, uint32_t tile, ui
     // Cayley, FP32: renormalise the trace to that of the initial density
     // matrix, in FP64, once per launch (the exact propagators preserve it:
     // the scattering matrix has zero column sums and U2 is unitary; this
-    // removes FP32 round-off drift)
+    // removes FP32 round-off drift). The pairs take the scaling as an
+    // increment, (s - 1) rho, accumulated error-free.
     if constexpr (ALGO == 2 && DF) {
         const pre::cay_layout L = pre::make_cay_layout(LEV);
 #pragma unroll
@@ -588,13 +592,16 @@ __device__ __forceinline__ void step_body(const kparams<T>& p, uint32_t tile, ui
             double tr = 0.0, target = 0.0;
 #pragma unroll
             for (int i = 0; i < LEV; i++) {
-                tr += (double) R[j][i];
+                tr += (double) R[j][i] + (double) Rl[j][i];
                 target += (double) cb[L.rho0 + i];
             }
             if (tr != 0.0 && fabs(tr / target - 1.0) < 1e-3) {
-                const float s = (float) (target / tr);
+                const float ds = (float) (target / tr - 1.0);
 #pragma unroll
-                for (int v = 0; v < DD; v++) R[j][v] *= s;
+                for (int v = 0; v < DD; v++) {
+                    df_acc(R[j][v], Rl[j][v], ds * R[j][v], ds * Rl[j][v]);
+                    df_renorm(R[j][v], Rl[j][v]);
+                }
             }
         }
     }
@@ -702,12 +709,12 @@ __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* a)
     return v;
 }
 
-// until the three progress counters reach `need` (polled together), then
-// an acquire fence; false when the wait ran out
+// until the three progress counters reach `need` (polled together, at most
+// `limit` times), then an acquire fence; false when the wait ran out
 __device__ __forceinline__ bool wait_progress(const uint32_t* a, const uint32_t* b, const uint32_t* c,
-                                              uint32_t need)
+                                              uint32_t need, uint32_t limit)
 {
-    for (uint32_t it = 0; it < PERSIST_WAIT_LIMIT; it++) {
+    for (uint32_t it = 0; it < limit; it++) {
         const uint32_t va = ld_relaxed(a), vb = ld_relaxed(b), vc = ld_relaxed(c);
         if ((int32_t) (va - need) >= 0 && (int32_t) (vb - need) >= 0 && (int32_t) (vc - need) >= 0) {
             asm volatile("fence.acq_rel.gpu;" ::: "memory");
@@ -731,7 +738,9 @@ __device__ __forceinline__ void persist_loop(const kparams<T>& p, const persist_
         const uint32_t k = w / q.n_tiles, i = w - k * q.n_tiles;
         if (threadIdx.x == 0) {
             const int2 nb = q.nb[i];
-            if (!wait_progress(q.prog + i, q.prog + nb.x, q.prog + nb.y, q.base + k))
+            // q.stall (tests only) asks for progress no tile reaches
+            if (!wait_progress(q.prog + i, q.prog + nb.x, q.prog + nb.y, q.base + k + q.stall,
+                               q.wait_limit ? q.wait_limit : PERSIST_WAIT_LIMIT))
                 atomicOr(p.status, STATUS_PERSIST_WAIT);
         }
         __syncthreads();

@@ -14,9 +14,10 @@ from tests import helpers
 pytestmark = pytest.mark.gpu
 
 # relative L2 error per record against the reference's FP64 result. FP32
-# keeps E, H and the coherence vector as float pairs; the Cayley density
-# matrix is plain FP32 (renormalised trace).
-TOL = {"fp64": 1e-9, "fp32": 1e-5, "fp32-cayley": 2e-4}
+# keeps E, H and the density state (coherence vector or Cayley density
+# matrix) as float pairs, with the field-free part of every step from the
+# FP64 precompute.
+TOL = {"fp64": 1e-9, "fp32": 1e-5}
 
 
 def _gpu_name(cpu_name, prec):
@@ -42,8 +43,7 @@ def test_gpu_matches_golden(native, case, prec):
     assert grid.num_timesteps == meta["num_timesteps"]
     assert sce.get_timestep_size() == meta["timestep_size"]
     errs = []
-    tol = TOL[prec + "-cayley"] if (prec == "fp32" and "cayley" in case) \
-        else TOL[prec]
+    tol = TOL[prec]
     for k, (a, b) in enumerate(zip(res, recs)):
         assert a.shape == b.shape
         errs.append(_check(a, b, tol, (case, k)))

@@ -167,3 +167,75 @@ def test_cayley_polarisation_weights(native, N):
     np.testing.assert_allclose(g, want, rtol=1e-12, atol=1e-12 * np.abs(want).max())
     r = np.random.default_rng(1).normal(size=N * N)
     assert g @ r == pytest.approx(P(r), rel=1e-12)
+
+
+@pytest.mark.parametrize("N,seed", [(2, 0), (3, 1), (4, 2), (6, 4)])
+def test_cayley_split_step_equals_reference_step(native, N, seed):
+    """The FP32 kernels' form of the Cayley step, rho + B0 rho + D(E(D
+    rho)) with E = Z (U0 + dU)^H + U0 Z^H, Z = dU D(rho),
+    dU = 2 i e A(e)^-1 W, equals the reference's step D(U2 D(rho) U2^H)
+    (algo_lindblad_reg_cayley.hpp:228-257) in FP64, for zero and nonzero
+    fields; B0l holds B0's FP32 rounding error."""
+    from mbsolve_gb300 import _native
+    dev, sce = setups.random_nlvl(N=N, num_gridpoints=16, num_timesteps=10,
+                                  seed=seed)
+    b = mb.to_pod(dev, sce)
+    mat = b.device.materials[0]
+    L = _native.material_layout("reg-cayley", N)
+    NN = N * N
+    c = _constants(native, "reg-cayley", mat, 2.5e-17)
+    pairs = [(j, k) for k in range(N) for j in range(k)]
+
+    def full(p):
+        m = np.diag(p[:N]).astype(complex)
+        for q, (j, k) in enumerate(pairs):
+            m[j, k] = p[N + 2 * q] + 1j * p[N + 2 * q + 1]
+            m[k, j] = np.conj(m[j, k])
+        return m
+
+    def pack(m):
+        out = np.zeros(NN)
+        out[:N] = np.real(np.diag(m))
+        for q, (j, k) in enumerate(pairs):
+            out[N + 2 * q] = m[j, k].real
+            out[N + 2 * q + 1] = m[j, k].imag
+        return out
+
+    K0 = full(c[L["kH0"]:L["kH0"] + NN])
+    K1 = full(c[L["kMu"]:L["kMu"] + NN])
+    dD1 = c[L["dD1"]:L["dD1"] + NN].reshape(N, N)
+    dD2 = c[L["dD2"]:L["dD2"] + len(pairs)]
+
+    def D(r):
+        o = r.copy()
+        o[:N] += dD1 @ r[:N]
+        for q in range(len(pairs)):
+            o[N + 2 * q:N + 2 * q + 2] *= 1.0 + dD2[q]
+        return o
+
+    def cmat(o):
+        return (c[o:o + NN] + 1j * c[o + NN:o + 2 * NN]).reshape(N, N)
+
+    U0 = cmat(L["U0"])
+    Wk = cmat(L["Wk"])
+    NP = L["NP"]
+    B0 = c[L["B0"]:L["B0"] + NN * NP].reshape(NN, NP)[:, :NN]
+    B0l = c[L["B0l"]:L["B0l"] + NN * NP].reshape(NN, NP)[:, :NN]
+    np.testing.assert_array_equal(B0l, B0 - B0.astype(np.float32))
+    I = np.eye(N)
+    rng = np.random.default_rng(seed)
+    for e in (0.0, 4e7, -9e8):
+        a = rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N))
+        rho = a @ a.conj().T
+        rho /= np.trace(rho).real
+        r = pack(rho)
+        K = K0 - e * K1
+        U2 = np.linalg.solve(I + 1j * K, I - 1j * K)
+        want = D(pack(U2 @ full(D(r)) @ U2.conj().T))
+        A = I + 1j * K
+        dU = 2j * e * np.linalg.solve(A, Wk)
+        np.testing.assert_allclose(U0 + dU, U2, rtol=0, atol=1e-14)
+        Z = dU @ full(D(r))
+        E = Z @ (U0 + dU).conj().T + U0 @ Z.conj().T
+        got = r + B0 @ r + D(pack(E))
+        np.testing.assert_allclose(got, want, rtol=0, atol=1e-14)
