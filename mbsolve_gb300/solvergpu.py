@@ -48,15 +48,25 @@ class solver_gpu_fdtd(mb.solver):
                                            bool(z.value)))
 
     def run(self):
-        _native.check(self._L.mbg_solver_run(self._h))
+        rc = self._L.mbg_solver_run(self._h)
+        if rc != T.MBG_OK:
+            # keep the error text: the copies below overwrite it
+            err = _native.MbgError(rc, self._L.mbg_last_error().decode())
         for k, res in enumerate(self._results):
             re = np.zeros(res.get_count())
             im = np.zeros(res.get_count())
-            _native.check(self._L.mbg_solver_copy_result(
-                self._h, k, re.ctypes.data_as(T.PD),
-                im.ctypes.data_as(T.PD)))
+            crc = self._L.mbg_solver_copy_result(
+                self._h, k, re.ctypes.data_as(T.PD), im.ctypes.data_as(T.PD))
+            if crc != T.MBG_OK:
+                if rc == T.MBG_OK:
+                    _native.check(crc)
+                break
             res._real = re
             res._imag = im
+        # a run that diverged (NaN/Inf) or whose device wait ran out raises
+        # after its results are in place, so that they can be inspected
+        if rc != T.MBG_OK:
+            raise err
 
     def __del__(self):
         h = getattr(self, "_h", None)
