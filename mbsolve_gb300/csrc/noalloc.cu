@@ -16,7 +16,6 @@
 // else. Calls that overlap on the GPU (different streams, different host
 // threads) race on the array and must not be issued.
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include "engine.hpp"
@@ -49,28 +48,21 @@ __global__ void precompute_noalloc_kernel(
     *code = rc;
 }
 
-// Device address of g_noalloc_ws, looked up once per device with that
-// device current (the host-side symbol is only a stand-in, not an address
-// a kernel can use).
-constexpr int MAX_DEVICES = 64;
-std::mutex g_addr_mutex;
-double* g_addr[MAX_DEVICES] = { nullptr };
-
-double* noalloc_workspace(int dev)
+// Device address of g_noalloc_ws on the current device. The host-side
+// symbol is only a stand-in, not an address a kernel can use. It is looked
+// up on every call, with the call's device current: a cached address would
+// go stale when the device's context is destroyed and created again (after
+// cudaDeviceReset the module loads anew and the array can move). The
+// lookup allocates nothing.
+double* noalloc_workspace()
 {
-    if (dev < 0 || dev >= MAX_DEVICES) throw mbg::invalid_argument("device ordinal out of range");
-    std::lock_guard<std::mutex> lk(g_addr_mutex);
-    if (!g_addr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_ws);
-        if (e != cudaSuccess) {
-            (void) cudaGetLastError();
-            throw mbg::cuda_error(std::string("CUDA: cudaGetSymbolAddress(workspace): ") +
-                                  cudaGetErrorString(e));
-        }
-        g_addr[dev] = static_cast<double*>(p);
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_ws);
+    if (e != cudaSuccess) {
+        (void) cudaGetLastError();
+        throw mbg::cuda_error(std::string("CUDA: cudaGetSymbolAddress(workspace): ") + cudaGetErrorString(e));
     }
-    return g_addr[dev];
+    return static_cast<double*>(p);
 }
 
 // Hermitian operator from the qm_operator packing (diagonal, then the upper
@@ -155,9 +147,7 @@ int mbg_material_constants_noalloc(
         fill_mat_in(*mat, N, timestep, in);
         if (kind == mbg::ALGO_CAYLEY && in.relax_kind != MBG_RELAX_LINDBLAD)
             throw mbg::invalid_argument("Unsupported superoperator!");
-        int devnum = 0;
-        MBG_CK(cudaGetDevice(&devnum));
-        double* ws = noalloc_workspace(devnum);
+        double* ws = noalloc_workspace();
         cudaStream_t s = static_cast<cudaStream_t>(stream);
         precompute_noalloc_kernel<<<1, 1, 0, s>>>(in, kind, N, ws, out_device);
         MBG_CK(cudaGetLastError());
