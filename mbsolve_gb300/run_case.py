@@ -5,6 +5,9 @@ counterpart of the reference tool's timing line, mbsolve-tool.cpp:672-696).
         --points 65536 --steps 2000 --solver gpu-fdtd-6lvl-cvr-rodr-fp32 \\
         [--runs 8] [--tuning C,NT,DEPTH]
 
+--setup ensemble_2lvl takes the first --runs runs of the batched 2-level
+ensemble (seed --seed) for --steps steps.
+
 Prints one JSON line: cell-updates/s over the timed steps (CUDA events on
 the engine's stream, after autotuning and a warm-up of 10 % of the steps),
 the tuning used and the device status.
@@ -26,22 +29,31 @@ def build(args, seed):
                                   num_timesteps=args.steps)
     if args.setup == "sit_2lvl":
         return setups.sit_2lvl(args.points, args.steps)
+    if args.setup == "ensemble_2lvl":
+        return setups.ensemble_2lvl(num_runs=args.runs,
+                                    num_timesteps=args.steps,
+                                    seed=args.seed)[0]
     raise SystemExit("unknown setup " + args.setup)
 
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--setup", default="random_nlvl",
-                    choices=["random_nlvl", "lambda_3lvl", "sit_2lvl"])
+                    choices=["random_nlvl", "lambda_3lvl", "sit_2lvl",
+                             "ensemble_2lvl"])
     ap.add_argument("--levels", type=int, default=6)
     ap.add_argument("--points", type=int, default=65536)
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--runs", type=int, default=1)
+    ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--solver", default="gpu-fdtd-6lvl-cvr-rodr-fp32")
     ap.add_argument("--tuning", default="", help="C,NT,DEPTH (default: autotune)")
     a = ap.parse_args(argv)
     mb.material.clear_library()
-    runs = [build(a, seed) for seed in range(a.runs)]
+    if a.setup == "ensemble_2lvl":
+        runs = build(a, a.seed)
+    else:
+        runs = [build(a, seed) for seed in range(a.runs)]
     tun = None
     if a.tuning:
         c, nt, d = (int(x) for x in a.tuning.split(","))

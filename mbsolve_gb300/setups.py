@@ -135,9 +135,52 @@ def marskar2011(N=6, num_gridpoints=8192, endtime=2e-12, length=1e-3):
     return dev, sce
 
 
-def tzenov2018_cpml(num_gridpoints=8192, endtime=2e-9):
+def tzenov2016(num_gridpoints=8192, endtime=0.2e-9, mirror=False,
+               seed=None, length=5e-3):
+    """Quantum cascade laser frequency comb, 5 levels (mbsolve-tool.cpp:
+    310-410): one 5 mm active region with semi-transparent end mirrors of
+    power reflectivity 0.8. The reference stores that boundary
+    (bc_field_reflectivity) and applies none (every solver keeps the PMC
+    boundary); mirror=True applies it instead (bc_field_mirror, opt-in, no
+    reference counterpart). The initial E field is random (the scenario's
+    density-only constructor); `seed` makes the draw reproducible. A
+    shorter `length` with num_gridpoints = 8192 length / 5 mm keeps the
+    reference's grid spacing (the records lie within 0.1 mm)."""
+    e = mb.E0
+    H = mb.qm_operator([0.10103 * e, 0.09677 * e, 0.09720 * e, 0.08129 * e,
+                        0.07633 * e],
+                       [0.0, 1.2329e-3 * e, -1.3447e-3 * e] + [0.0] * 7)
+    # dipole between levels 2 and 3 (upper index (2, 3), column-major)
+    u = mb.qm_operator([0.0] * 5, [0.0] * 5 + [-e * 4e-9] + [0.0] * 4)
+    scat = [[0.0, 0.4947e12, 0.0974e12, 0.8116e12, 1.0410e12],
+            [0.8245e12, 0.0, 0.1358e12, 0.6621e12, 1.1240e12],
+            [0.0229e12, 0.0469e12, 0.0, 0.0794e12, 0.0357e12],
+            [0.0047e12, 0.0029e12, 0.1252e12, 0.0, 0.2810e12],
+            [0.0049e12, 0.0049e12, 0.1101e12, 0.4949e12, 0.0]]
+    inj_ull = 1.0 / 1.6e-12
+    other = 1.0 / 4.8e-12
+    deph = [0.0, inj_ull, inj_ull] + [other] * 7
+    qm = mb.qm_description(5.6e21, H, u,
+                           mb.qm_lindblad_relaxation(scat, deph))
+    ar = _material("AR", qm, 19.35, 0.9, 1300)
+    bc = (mb.bc_field_mirror if mirror else mb.bc_field_reflectivity)(0.8,
+                                                                      0.8)
+    dev = mb.device("tzenov2016", bc)
+    dev.add_region(mb.region("Active region", ar, 0, length))
+    sce = mb.scenario("basic", num_gridpoints, endtime,
+                      mb.qm_operator([0.0, 0.0, 1.0, 0.0, 0.0]))
+    if seed is not None:
+        sce.set_ic_electric(mb.ic_field_random(seed=seed))
+    sce.add_record(mb.record("e0", mb.record.electric, 1, 1, 0.0, 0.0))
+    for i in range(1, 6):
+        sce.add_record(mb.record("d%d%d" % (i, i), mb.record.density, i, i,
+                                 0.0, 0.1e-3))
+    return dev, sce
+
+
+def tzenov2018_cpml(num_gridpoints=8192, endtime=2e-9, seed=None):
     """Colliding-pulse mode locking, absorber between two gain sections
-    (mbsolve-tool.cpp:411-478)."""
+    (mbsolve-tool.cpp:411-478); `seed` as in tzenov2016."""
     qm_gain = mb.qm_desc_2lvl(5e21, 2 * mb.PI * 3.4e12, 2e-9, 1.0 / 10e-12,
                               1.0 / 200e-15, 1.0)
     qm_abs = mb.qm_desc_2lvl(1e21, 2 * mb.PI * 3.4e12, 6e-9, 1.0 / 3e-12,
@@ -150,6 +193,8 @@ def tzenov2018_cpml(num_gridpoints=8192, endtime=2e-9):
     dev.add_region(mb.region("Gain L", mat_gain, 0.625e-3, 1.125e-3))
     sce = mb.scenario("basic", num_gridpoints, endtime,
                       mb.qm_operator([0.5, 0.5], [0.001]))
+    if seed is not None:
+        sce.set_ic_electric(mb.ic_field_random(seed=seed))
     sce.add_record(mb.record("inv12", 1e-12))
     sce.add_record(mb.record("e", 1e-12))
     sce.add_record(mb.record("e0", mb.record.electric, 1, 1, 0.0, 0.0))

@@ -15,7 +15,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    # default: $MBSOLVE_REFERENCE, else a checkout named "reference" beside
+    # this repository
+    root = sys.argv[1] if len(sys.argv) > 1 else (
+        os.environ.get("MBSOLVE_REFERENCE") or
+        os.path.join(HERE, "..", "..", "..", "..", "reference"))
     d = os.path.join(root, "tools", "reference-data")
     out = {}
     for key, name in [("ziolkowski1995_inv12_row75", "ziolkowski1995-2.csv"),

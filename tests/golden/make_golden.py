@@ -4,7 +4,8 @@ reference tree (oracle/_ref, built by oracle/build_ref.sh), instantiated
 with the oracle's Eigen-free Lindblad algorithms. One OpenMP thread (the
 reference applies soft sources once per thread).
 
-Usage: python tests/golden/make_golden.py [reference-root]
+Usage: python tests/golden/make_golden.py [--reference ROOT] [case ...]
+(default: every case)
 """
 import json
 import os
@@ -40,16 +41,30 @@ CASES = {
                       dict(num_gridpoints=512, num_timesteps=3000)),
     "lambda_cvr": ("cpu-fdtd-3lvl-cvr-rodr", "lambda_3lvl",
                    dict(num_gridpoints=512, num_timesteps=3000)),
+    # the QCL comb preset at the reference's grid spacing on a 0.31 mm
+    # device (random initial field, seeded), both forms
+    "tzenov2016_cvr": ("cpu-fdtd-5lvl-cvr-rodr", "tzenov2016",
+                       dict(num_gridpoints=512, endtime=12e-12, seed=1,
+                            length=5e-3 * 511 / 8191)),
+    "tzenov2016_cayley": ("cpu-fdtd-5lvl-reg-cayley", "tzenov2016",
+                          dict(num_gridpoints=512, endtime=12e-12, seed=1,
+                               length=5e-3 * 511 / 8191)),
+    # colliding-pulse mode locking: gain, absorber, gain (random initial
+    # field, seeded)
+    "tzenov2018_cvr": ("cpu-fdtd-2lvl-cvr-rodr", "tzenov2018_cpml",
+                       dict(num_gridpoints=512, endtime=30e-12, seed=1)),
 }
 
 
-def main(ref_root=None):
+def main(ref_root=None, only=()):
     if ref_root:
         os.environ["MBSOLVE_REFERENCE"] = ref_root
     from mbsolve_gb300 import lib as mb
     from tests import helpers
     out_dir = os.path.dirname(os.path.abspath(__file__))
     for case, (solver, setup, kw) in CASES.items():
+        if only and case not in only:
+            continue
         mb.material.clear_library()
         spec = {"setup": setup, "kw": kw}
         dev, sce = helpers.build_setup(spec)
@@ -69,4 +84,9 @@ def main(ref_root=None):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else None)
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=None)
+    ap.add_argument("cases", nargs="*")
+    a = ap.parse_args()
+    main(a.reference, tuple(a.cases))
