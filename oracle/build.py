@@ -5,6 +5,15 @@ oracle/_build/libmb_oracle.so, and, when the reference tree is present,
 oracle/_ref/libmbref.so from the reference's own sources (build_ref.sh).
 Flags keep results identical across x86 and Arm: no -march, no FMA
 contraction.
+
+build_baseline() builds the same source a second time, as the CPU
+baseline, with the flags of the reference's own solver-cpu build
+(solver-cpu/CMakeLists.txt: -O3, OpenMP, USE_OMP_SIMD=1, the compiler's
+default FP contraction) into oracle/_build/libmb_baseline.so. The
+reference's -march=native is replaced by the host CPU's named target
+(Arm: -mcpu of the Neoverse core the machine reports, e.g. neoverse-v2 on
+Grace; x86: -march=x86-64-v3), so that the build does not depend on the
+machine beyond its CPU model. Only timed, never used as the checker.
 """
 import os
 import subprocess
@@ -12,8 +21,13 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libmb_oracle.so")
+BASELINE_SO = os.path.join(HERE, "_build", "libmb_baseline.so")
 REF_SO = os.path.join(HERE, "_ref", "libmbref.so")
-REFERENCE_ROOT = os.environ.get("MBSOLVE_REFERENCE", "/root/reference")
+REF_BASELINE_SO = os.path.join(HERE, "_ref", "libmbref_baseline.so")
+# the mbsolve source tree: $MBSOLVE_REFERENCE, else a checkout named
+# "reference" beside this repository
+REFERENCE_ROOT = os.environ.get("MBSOLVE_REFERENCE") or os.path.normpath(
+    os.path.join(HERE, "..", "..", "reference"))
 
 
 def _stale(target, sources):
@@ -54,20 +68,85 @@ def build_oracle(force=False):
     return ORACLE_SO
 
 
-def build_reference(force=False):
-    """Build oracle/_ref from the reference tree; None when it is absent."""
+def _cxx_accepts(flag):
+    r = subprocess.run([os.environ.get("CXX", "g++"), flag, "-x", "c++",
+                        "-fsyntax-only", "-"], input="int main(){}",
+                       capture_output=True, text=True)
+    return r.returncode == 0
+
+
+def cpu_target_flags():
+    """The named target for this host CPU (see the module docstring)."""
+    import platform
+    m = platform.machine()
+    if m in ("aarch64", "arm64"):
+        part = None
+        try:
+            with open("/proc/cpuinfo") as f:
+                for line in f:
+                    if line.lower().startswith("cpu part"):
+                        part = line.split(":")[1].strip().lower()
+                        break
+        except OSError:
+            pass
+        # Arm Ltd. part numbers of the Neoverse cores
+        names = {"0xd4f": "neoverse-v2", "0xd40": "neoverse-v1",
+                 "0xd0c": "neoverse-n1", "0xd49": "neoverse-n2",
+                 "0xd84": "neoverse-v3"}
+        flag = "-mcpu=" + names.get(part, "neoverse-v2")
+        return [flag] if _cxx_accepts(flag) else []
+    if m in ("x86_64", "AMD64"):
+        return ["-march=x86-64-v3"] if _cxx_accepts("-march=x86-64-v3") \
+            else []
+    return []
+
+
+def baseline_flags():
+    return ["-O3", "-fopenmp", "-DUSE_OMP_SIMD=1"] + cpu_target_flags()
+
+
+def build_baseline(force=False):
+    """The CPU-baseline build of mb_oracle.cpp (reference flags)."""
+    src = os.path.join(HERE, "mb_oracle.cpp")
+    if not _arch_ok(BASELINE_SO):
+        force = True
+    hdr = os.path.join(HERE, "..", "include", "mbsolve_gb300.h")
+    if not force and not _stale(BASELINE_SO, [src, hdr, __file__]):
+        return BASELINE_SO
+    os.makedirs(os.path.dirname(BASELINE_SO), exist_ok=True)
+    tmp = BASELINE_SO + ".tmp%d" % os.getpid()
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-fPIC", "-shared"] + \
+        baseline_flags() + [src, "-o", tmp]
+    subprocess.check_call(cmd)
+    os.replace(tmp, BASELINE_SO)
+    _write_arch(BASELINE_SO)
+    return BASELINE_SO
+
+
+def build_reference(force=False, baseline=False):
+    """Build oracle/_ref from the reference tree; None when it is absent.
+    baseline=True: the same sources with the CPU baseline's flags
+    (libmbref_baseline.so), to calibrate the restated baseline against the
+    reference's own loops on a machine that has the reference tree."""
     if not os.path.isdir(os.path.join(REFERENCE_ROOT, "mbsolve-lib", "src")):
         return None
+    out = REF_BASELINE_SO if baseline else REF_SO
     srcs = [os.path.join(HERE, f) for f in
-            ("ref_driver.cpp", "ref_algos.hpp", "mb_oracle.cpp")]
-    if not force and _arch_ok(REF_SO) and not _stale(REF_SO, srcs):
-        return REF_SO
+            ("ref_driver.cpp", "ref_algos.hpp", "mb_oracle.cpp",
+             "build_ref.sh")]
+    if not force and _arch_ok(out) and not _stale(out, srcs):
+        return out
+    env = dict(os.environ)
+    if baseline:
+        env["REF_CXXFLAGS"] = " ".join(baseline_flags())
+        env["REF_LIB"] = os.path.basename(out)
     subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"),
-                           REFERENCE_ROOT])
-    _write_arch(REF_SO)
-    return REF_SO
+                           REFERENCE_ROOT], env=env)
+    _write_arch(out)
+    return out
 
 
 if __name__ == "__main__":
     print(build_oracle(force="-f" in sys.argv))
+    print(build_baseline(force="-f" in sys.argv))
     print(build_reference(force="-f" in sys.argv))

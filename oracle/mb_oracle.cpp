@@ -745,8 +745,10 @@ static rodr_consts rodr_constants(const qm_desc* q, int N, real dt)
     return sc;
 }
 
-/* algo_lindblad_cvr_rodr.hpp:234-268 */
-static void rodr_update(
+/* algo_lindblad_cvr_rodr.hpp:234-268. Inlined into callers with a constant
+ * N (rodr_update_n), as the reference's update is instantiated per level
+ * count; the arithmetic and its order are the same for every N. */
+__attribute__((always_inline)) static inline void rodr_update(
     const rodr_consts& sc,
     int N,
     real* d,
@@ -754,7 +756,7 @@ static void rodr_update(
     real* p_t)
 {
     if (!sc.has_qm) return;
-    int V = N * N - 1;
+    const int V = N * N - 1;
     real x[64], d1[64], d2[64];
     for (int i = 0; i < V; i++) x[i] = d[i] + sc.d_in[i];
     for (int i = 0; i < V; i++) {
@@ -762,8 +764,9 @@ static void rodr_update(
         for (int j = 0; j < V; j++) s += sc.A1(i, j) * x[j];
         d1[i] = s - sc.d_in[i];
     }
-    /* A2 */
-    std::vector<real> A2((size_t) V * V, 0.0);
+    /* A2 (on the stack, like the reference's fixed-size matrices) */
+    real A2[35 * 35];
+    for (int i = 0; i < V * V; i++) A2[i] = 0.0;
     if (N == 2) {
         real th = sc.theta_1;
         real a = 0.0, b = 0.0;
@@ -801,6 +804,24 @@ static void rodr_update(
         acc += sc.v[i] * (s + sc.d_eq[i]);
     }
     *p_t = sc.M_CP * acc;
+}
+
+template<int NL>
+static void rodr_update_t(const rodr_consts& sc, real* d, real e, real* p_t)
+{
+    rodr_update(sc, NL, d, e, p_t);
+}
+
+static void rodr_update_n(const rodr_consts& sc, int N, real* d, real e, real* p_t)
+{
+    switch (N) {
+    case 2: rodr_update_t<2>(sc, d, e, p_t); break;
+    case 3: rodr_update_t<3>(sc, d, e, p_t); break;
+    case 4: rodr_update_t<4>(sc, d, e, p_t); break;
+    case 5: rodr_update_t<5>(sc, d, e, p_t); break;
+    case 6: rodr_update_t<6>(sc, d, e, p_t); break;
+    default: rodr_update(sc, N, d, e, p_t);
+    }
 }
 
 /* --------------------------------------------------- Lindblad: Cayley */
@@ -1293,7 +1314,13 @@ static void run(solver* s, int threads, uint32_t max_steps)
 #pragma omp parallel num_threads(threads)
     {
         for (uint32_t t = 0; t < steps; t++) {
+            // USE_OMP_SIMD (the CPU-baseline build): the reference's
+            // vectorised field loops (solver_cpu_fdtd.tpp:233-236, 258-261)
+#if USE_OMP_SIMD
+#pragma omp for simd schedule(static)
+#else
 #pragma omp for schedule(static)
+#endif
             for (int64_t i = 0; i < n; i++)
                 E[i] = fa[i] * E[i] +
                     fb[i] * (-ga[i] * P[i] + (H[i + 1] - H[i]) * dxi);
@@ -1304,7 +1331,11 @@ static void run(solver* s, int threads, uint32_t max_steps)
                 else if (src.type == MBG_SOURCE_SOFT)
                     E[src.x_idx] += src.values[t];
             }
+#if USE_OMP_SIMD
+#pragma omp for simd schedule(static)
+#else
 #pragma omp for schedule(static)
+#endif
             for (int64_t i = 1; i < n; i++) H[i] += fc[i] * (E[i] - E[i - 1]);
 #pragma omp single
             {
@@ -1314,7 +1345,7 @@ static void run(solver* s, int threads, uint32_t max_steps)
             if (s->algo == ALGO_RODR) {
 #pragma omp for schedule(static)
                 for (int64_t i = 0; i < n; i++)
-                    rodr_update(
+                    rodr_update_n(
                         s->rodr[mi[i]], s->N, &s->d_cvr[i * s->V], E[i], &P[i]);
             } else if (s->algo == ALGO_CAYLEY) {
 #pragma omp for schedule(static)
@@ -1399,6 +1430,10 @@ static void run_red(solver* s, int threads, uint32_t max_steps, int ol)
             const uint32_t* mi = s->mat_idx.data() + lo;
             for (uint32_t k = 0; k < nsub; k++) {
                 const uint32_t step = t0 + k;
+                // (red.tpp:300-301, 318-319 under USE_OMP_SIMD)
+#if USE_OMP_SIMD
+#pragma omp simd
+#endif
                 for (int64_t i = 0; i < m; i++)
                     Ep[i] = fa[i] * Ep[i] + fb[i] * (-ga[i] * Pp[i] + (Hp[i + 1] - Hp[i]) * dxi);
                 for (const auto& src : s->sources) {
@@ -1409,12 +1444,15 @@ static void run_red(solver* s, int threads, uint32_t max_steps, int ol)
                     else if (src.type == MBG_SOURCE_SOFT)
                         Ep[x - lo] += src.values[step];
                 }
+#if USE_OMP_SIMD
+#pragma omp simd
+#endif
                 for (int64_t i = 1; i < m; i++) Hp[i] += fc[i] * (Ep[i] - Ep[i - 1]);
                 if (lo == 0) Hp[0] = s->wall_l != 0 ? s->wall_l * Ep[0] : 0;
                 if (hi == n) Hp[m] = s->wall_r != 0 ? -s->wall_r * Ep[m - 1] : 0;
                 if (s->algo == ALGO_RODR) {
                     for (int64_t i = 0; i < m; i++)
-                        rodr_update(s->rodr[mi[i]], s->N, &D[i * V], Ep[i], &Pp[i]);
+                        rodr_update_n(s->rodr[mi[i]], s->N, &D[i * V], Ep[i], &Pp[i]);
                 } else if (s->algo == ALGO_CAYLEY) {
                     for (int64_t i = 0; i < m; i++)
                         cayley_update(s->cay[mi[i]], R[i], Ep[i], &Pp[i]);

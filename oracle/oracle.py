@@ -14,43 +14,55 @@ from . import build as _build
 from mbsolve_gb300 import capi_types as T
 
 _lib = None
-_ref = None
+_base = None
+_ref = {}
 
 
 def lib():
     global _lib
     if _lib is None:
-        path = _build.build_oracle()
-        L = C.CDLL(path)
-        L.mbo_last_error.restype = C.c_char_p
-        L.mbo_create.argtypes = [C.c_char_p, C.c_uint32,
-                                 C.POINTER(T.mbg_device),
-                                 C.POINTER(T.mbg_scenario),
-                                 C.POINTER(C.c_void_p)]
-        L.mbo_grid.argtypes = [C.c_void_p, C.POINTER(T.mbg_grid)]
-        L.mbo_run.argtypes = [C.c_void_p, C.c_int, C.c_uint32]
-        L.mbo_run_red.argtypes = [C.c_void_p, C.c_int, C.c_uint32, C.c_int]
-        L.mbo_num_results.argtypes = [C.c_void_p, C.POINTER(C.c_uint32)]
-        L.mbo_result_shape.argtypes = [C.c_void_p, C.c_uint32,
-                                       C.POINTER(C.c_uint32),
-                                       C.POINTER(C.c_uint32),
-                                       C.POINTER(C.c_int32)]
-        L.mbo_copy_result.argtypes = [C.c_void_p, C.c_uint32, T.PD, T.PD]
-        L.mbo_state.argtypes = [C.c_void_p, T.PD, T.PD, T.PD, T.PD]
-        L.mbo_destroy.argtypes = [C.c_void_p]
-        L.mbo_expm.argtypes = [C.c_int, T.PD, T.PD]
-        L.mbo_rodr_constants.argtypes = [C.POINTER(T.mbg_qm), C.c_double,
-                                         C.c_double] + [T.PD] * 9
-        _lib = L
+        _lib = _bind(C.CDLL(_build.build_oracle()))
     return _lib
 
 
-def ref_lib():
+def baseline_lib():
+    """The same restatement built with the reference's own solver-cpu
+    flags (oracle/build.py build_baseline): the timed CPU baseline."""
+    global _base
+    if _base is None:
+        _base = _bind(C.CDLL(_build.build_baseline()))
+    return _base
+
+
+def _bind(L):
+    L.mbo_last_error.restype = C.c_char_p
+    L.mbo_create.argtypes = [C.c_char_p, C.c_uint32,
+                             C.POINTER(T.mbg_device),
+                             C.POINTER(T.mbg_scenario),
+                             C.POINTER(C.c_void_p)]
+    L.mbo_grid.argtypes = [C.c_void_p, C.POINTER(T.mbg_grid)]
+    L.mbo_run.argtypes = [C.c_void_p, C.c_int, C.c_uint32]
+    L.mbo_run_red.argtypes = [C.c_void_p, C.c_int, C.c_uint32, C.c_int]
+    L.mbo_num_results.argtypes = [C.c_void_p, C.POINTER(C.c_uint32)]
+    L.mbo_result_shape.argtypes = [C.c_void_p, C.c_uint32,
+                                   C.POINTER(C.c_uint32),
+                                   C.POINTER(C.c_uint32),
+                                   C.POINTER(C.c_int32)]
+    L.mbo_copy_result.argtypes = [C.c_void_p, C.c_uint32, T.PD, T.PD]
+    L.mbo_state.argtypes = [C.c_void_p, T.PD, T.PD, T.PD, T.PD]
+    L.mbo_destroy.argtypes = [C.c_void_p]
+    L.mbo_expm.argtypes = [C.c_int, T.PD, T.PD]
+    L.mbo_rodr_constants.argtypes = [C.POINTER(T.mbg_qm), C.c_double,
+                                     C.c_double] + [T.PD] * 9
+    return L
+
+
+def ref_lib(baseline=False):
     """The reference-built library, or None when the reference tree is
-    absent (the GPU machines have only the oracle restatement)."""
-    global _ref
-    if _ref is None:
-        path = _build.build_reference()
+    absent (the GPU machines have only the oracle restatement); baseline:
+    the build with the CPU baseline's flags."""
+    if baseline not in _ref:
+        path = _build.build_reference(baseline=baseline)
         if path is None:
             return None
         L = C.CDLL(path)
@@ -66,8 +78,8 @@ def ref_lib():
                                        C.POINTER(C.c_int32)]
         L.mbr_copy_result.argtypes = [C.c_void_p, C.c_uint32, T.PD, T.PD]
         L.mbr_destroy.argtypes = [C.c_void_p]
-        _ref = L
-    return _ref
+        _ref[baseline] = L
+    return _ref[baseline]
 
 
 def _ptr(a):
@@ -82,8 +94,8 @@ class OracleRun:
     """One oracle solver: create, run (optionally a bounded number of
     steps), read grid and results."""
 
-    def __init__(self, algo, num_levels, bundle):
-        L = lib()
+    def __init__(self, algo, num_levels, bundle, baseline=False):
+        L = baseline_lib() if baseline else lib()
         self._L = L
         self._bundle = bundle
         h = C.c_void_p()
@@ -144,8 +156,8 @@ class OracleRun:
 class ReferenceRun:
     """The reference's own solver (e.g. "cpu-fdtd-2lvl-cvr-rodr")."""
 
-    def __init__(self, name, bundle):
-        L = ref_lib()
+    def __init__(self, name, bundle, baseline=False):
+        L = ref_lib(baseline)
         if L is None:
             raise OracleError("reference tree not available")
         self._L = L

@@ -9,7 +9,8 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("MBSOLVE_REFERENCE", "/root/reference")
+REF = os.environ.get("MBSOLVE_REFERENCE") or os.path.normpath(
+    os.path.join(ROOT, "..", "reference"))
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "mbsolve-lib", "src")),
