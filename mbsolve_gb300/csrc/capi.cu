@@ -462,7 +462,8 @@ size_t mbg_material_layout(const char* algo, uint32_t N, char* buf, size_t len)
           << "\nkH0=" << L.kH0 << "\nkMu=" << L.kMu << "\nW0=" << L.W0 << "\nMn=" << L.Mn << "\ndD1=" << L.dD1
           << "\nd1=" << L.d1 << "\ndD2=" << L.dD2 << "\nd2=" << L.d2 << "\nrho0=" << L.rho0
           << "\ngP=" << L.gP << "\nstage64=" << L.stage64 << "\nU0=" << L.U0 << "\nWk=" << L.Wk
-          << "\nNP=" << L.NP << "\nB0=" << L.B0 << "\nB0l=" << L.B0l << "\nstride=" << L.stride;
+          << "\nNP=" << L.NP << "\nB0=" << L.B0 << "\nB0l=" << L.B0l << "\nblockB0=" << L.blockB0
+          << "\nstride=" << L.stride;
     }
     std::string t = s.str();
     if (buf && len) {

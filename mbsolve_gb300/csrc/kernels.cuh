@@ -953,16 +953,33 @@ __device__ __forceinline__ void cayley_update_df(float (&rh)[N * N], float (&rl)
         inc[N + 2 * q] = fmaf(dd, ev[N + 2 * q], ev[N + 2 * q]);
         inc[N + 2 * q + 1] = fmaf(dd, ev[N + 2 * q + 1], ev[N + 2 * q + 1]);
     }
+    if (cf[L.blockB0] != 0.0f) {
+        // diagonal H0: B0 is block-diagonal (populations; each coherence's
+        // 2 x 2 block), the same sums without their exact zero terms
 #pragma unroll
-    for (int v = 0; v < NN; v++) {
-        float a = inc[v], b = 0.0f;
+        for (int v = 0; v < NN; v++) {
+            float a = inc[v], b = 0.0f;
+            const int w0 = v < N ? 0 : N + ((v - N) & ~1), w1 = v < N ? N : w0 + 2;
 #pragma unroll
-        for (int w = 0; w < NN; w++) {
-            a = fmaf(cf[L.B0 + v * L.NP + w], rh[w], a);
-            b = fmaf(cf[L.B0l + v * L.NP + w], rh[w], b);
+            for (int w = w0; w < w1; w++) {
+                a = fmaf(cf[L.B0 + v * L.NP + w], rh[w], a);
+                b = fmaf(cf[L.B0l + v * L.NP + w], rh[w], b);
+            }
+            inc[v] = a;
+            incl[v] = b;
         }
-        inc[v] = a;
-        incl[v] = b;
+    } else {
+#pragma unroll
+        for (int v = 0; v < NN; v++) {
+            float a = inc[v], b = 0.0f;
+#pragma unroll
+            for (int w = 0; w < NN; w++) {
+                a = fmaf(cf[L.B0 + v * L.NP + w], rh[w], a);
+                b = fmaf(cf[L.B0l + v * L.NP + w], rh[w], b);
+            }
+            inc[v] = a;
+            incl[v] = b;
+        }
     }
     float acc = 0.0f;
 #pragma unroll

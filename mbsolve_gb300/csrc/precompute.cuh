@@ -205,7 +205,9 @@ struct cay_layout {
     int a, b, cH, gam, has_qm;
     int kH0, kMu, W0, Mn, dD1, d1, dD2, d2, rho0, gP;
     int stage64;  // leading part the FP64 kernels use and stage
-    int U0, Wk, NP, B0, B0l, stride;
+    int U0, Wk, NP, B0, B0l;
+    int blockB0;  // 1: H0 is diagonal and B0 block-diagonal (see cay_free_step)
+    int stride;
 };
 
 MBG_HD cay_layout make_cay_layout(int N)
@@ -251,6 +253,8 @@ MBG_HD cay_layout make_cay_layout(int N)
     o += N * N * L.NP;
     L.B0l = o;
     o += N * N * L.NP;
+    L.blockB0 = o;
+    o += 1;
     L.stride = (o + 3) & ~3;
     return L;
 }
@@ -1129,7 +1133,11 @@ MBG_HD void cay_dissipation_increment(const cay_layout& L, const double* out, co
 // The field-free part of the FP32 Cayley step (see cay_layout): U0, W and
 // B0 = D Ad(U0) D - I from kH0, kMu, dD1 and dD2, all in FP64. B0's
 // columns are formed as sums of small increments (never as T0 e - e), so
-// its entries keep their relative accuracy however small the rates.
+// its entries keep their relative accuracy however small the rates. With
+// a diagonal H0 (every preset but the random media) U0 is diagonal and B0
+// block-diagonal, exactly: populations mix among themselves, each
+// coherence (re, im) only with itself; blockB0 = 1 lets the kernels skip
+// the zero blocks (the same sums without exact zero terms).
 // ws: 17 N^2 doubles.
 MBG_HD void cay_free_step(const cay_layout& L, double* ws, double* out)
 {
@@ -1175,6 +1183,10 @@ MBG_HD void cay_free_step(const cay_layout& L, double* ws, double* out)
             out[L.Wk + j * N + k] = s.re;
             out[L.Wk + NN + j * N + k] = s.im;
         }
+    bool diag = true;
+    for (int q = 0; q < L.P; q++)
+        if (out[L.kH0 + N + 2 * q] != 0.0 || out[L.kH0 + N + 2 * q + 1] != 0.0) diag = false;
+    out[L.blockB0] = diag ? 1.0 : 0.0;
     // columns of B0: e_v -> (D - I) e_v + pack(Ad(U0) s - s) + (D - I) tau,
     // s = D e_v, tau = Ad(U0) s
     for (int v = 0; v < NN; v++) {

@@ -239,3 +239,32 @@ def test_cayley_split_step_equals_reference_step(native, N, seed):
         E = Z @ (U0 + dU).conj().T + U0 @ Z.conj().T
         got = r + B0 @ r + D(pack(E))
         np.testing.assert_allclose(got, want, rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("setup,kw", [
+    ("lambda_3lvl", dict(num_gridpoints=16, num_timesteps=10)),
+    ("marskar2011", dict(N=5, num_gridpoints=16, endtime=1e-13)),
+    ("random_nlvl", dict(N=3, num_gridpoints=16, num_timesteps=10))])
+def test_cayley_block_structure_flag(native, setup, kw):
+    """With a diagonal H0 the field-free matrix B0 is block-diagonal, its
+    other entries exactly zero, and the block flag is set (the kernels then
+    skip those zeros); a Hamiltonian with couplings keeps the dense path."""
+    from mbsolve_gb300 import _native
+    dev, sce = helpers.build_setup({"setup": setup, "kw": kw})
+    b = mb.to_pod(dev, sce)
+    mat = b.device.materials[0]
+    N = mat.qm.contents.num_levels
+    L = _native.material_layout("reg-cayley", N)
+    c = _constants(native, "reg-cayley", mat, 2.5e-17)
+    NN, NP = N * N, L["NP"]
+    B0 = c[L["B0"]:L["B0"] + NN * NP].reshape(NN, NP)[:, :NN]
+    mask = np.zeros((NN, NN), bool)
+    mask[:N, :N] = True
+    for q in range((NN - N) // 2):
+        mask[N + 2 * q:N + 2 * q + 2, N + 2 * q:N + 2 * q + 2] = True
+    diag = setup != "random_nlvl"
+    assert c[L["blockB0"]] == (1.0 if diag else 0.0)
+    if diag:
+        assert np.all(B0[~mask] == 0.0)
+    else:
+        assert np.any(B0[~mask] != 0.0)
