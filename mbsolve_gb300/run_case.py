@@ -3,7 +3,7 @@ counterpart of the reference tool's timing line, mbsolve-tool.cpp:672-696).
 
     python -m mbsolve_gb300.run_case --setup random_nlvl --levels 6 \\
         --points 65536 --steps 2000 --solver gpu-fdtd-6lvl-cvr-rodr-fp32 \\
-        [--runs 8] [--tuning C,NT,DEPTH]
+        [--runs 8] [--tuning C,NT,DEPTH[,PERSISTENT]]
 
 --setup ensemble_2lvl takes the first --runs runs of the batched 2-level
 ensemble (seed --seed) for --steps steps.
@@ -47,7 +47,10 @@ def main(argv=None):
     ap.add_argument("--runs", type=int, default=1)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--solver", default="gpu-fdtd-6lvl-cvr-rodr-fp32")
-    ap.add_argument("--tuning", default="", help="C,NT,DEPTH (default: autotune)")
+    ap.add_argument("--tuning", default="",
+                    help="C,NT,DEPTH[,PERSISTENT] (default: autotune; "
+                         "PERSISTENT 1 = persistent kernel, 2 = one launch "
+                         "per DEPTH steps)")
     a = ap.parse_args(argv)
     mb.material.clear_library()
     if a.setup == "ensemble_2lvl":
@@ -56,8 +59,9 @@ def main(argv=None):
         runs = [build(a, seed) for seed in range(a.runs)]
     tun = None
     if a.tuning:
-        c, nt, d = (int(x) for x in a.tuning.split(","))
-        tun = ensemble.tuning(c, nt, d)
+        v = [int(x) for x in a.tuning.split(",")]
+        tun = ensemble.tuning(v[0], v[1], v[2],
+                              persistent=v[3] if len(v) > 3 else 0)
     e = ensemble.ensemble(a.solver, runs, tun)
     warm = max(1, a.steps // 10)
     timed = a.steps - warm
