@@ -82,6 +82,12 @@ typedef struct mbg_gemm_desc {
     const float* bias;
     float* pre;
     const float* gate;
+    /* optional second output (NULL: none; STORE mode only): the same
+     * values as BF16 at c2 + z c2_sz + i c2_sm + j c2_sn, e.g. the
+     * transposed copy of an activation that the next product reads with
+     * K contiguous */
+    void* c2;
+    int64_t c2_sm, c2_sn, c2_sz;
 } mbg_gemm_desc;
 
 int mbg_fno_gemm(const mbg_gemm_desc* d, void* stream);

@@ -188,4 +188,6 @@ class mbg_gemm_desc(C.Structure):
         ("bias", C.c_void_p),
         ("pre", C.c_void_p),
         ("gate", C.c_void_p),
+        ("c2", C.c_void_p),
+        ("c2_sm", C.c_int64), ("c2_sn", C.c_int64), ("c2_sz", C.c_int64),
     ]

@@ -5,15 +5,20 @@
 // gradients) are small strided GEMMs. One tensor-core kernel serves all of
 // them: a 128 x 64 output tile per CTA, accumulated in tensor memory (TMEM)
 // by tcgen05.mma (kind::f16, BF16 operands, FP32 accumulator), K in blocks
-// of 64 staged in shared memory in two stages. Operands are gathered with
-// plain loads (any strides, FP32 or BF16, converted to BF16 on the way) and
-// written into the no-swizzle K-major core-matrix layout the tensor core
-// reads: 8 rows x 16 bytes per core matrix, core matrices 128 bytes apart
-// along K (leading byte offset) and 1024 bytes apart along M/N (stride byte
-// offset). One elected thread issues the MMAs; tcgen05.commit arrives on the
-// stage's mbarrier when they have read the stage. Every wait is bounded: on
-// time-out the kernel records it in the status word and returns after
-// freeing its TMEM.
+// of 64 staged in shared memory. Operands are written into the no-swizzle K-major
+// core-matrix layout the tensor core reads: 8 rows x 16 bytes per core
+// matrix, core matrices 128 bytes apart along K (leading byte offset) and
+// 1024 bytes apart along M/N (stride byte offset). When every operand of a
+// product is BF16 with K contiguous (16-byte aligned rows), each 16-byte
+// chunk is copied asynchronously (cp.async, zero-filled outside the
+// operand) into a ring of four stages filled two blocks ahead of the MMAs;
+// otherwise it is gathered with plain loads (any strides, FP32 or BF16,
+// converted to BF16 on the way) into two stages, each loaded while the
+// MMAs of the other run (the smaller footprint keeps four CTAs per SM for
+// the short-K gathers of training). One elected thread issues the MMAs;
+// tcgen05.commit arrives on the stage's mbarrier when they have read the
+// stage. Every wait is bounded: on time-out the kernel records it in the
+// status word and returns after freeing its TMEM.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -37,12 +42,15 @@ constexpr int BM = 128;          // rows of a tile (TMEM lanes)
 constexpr int BN = 64;           // columns of a tile (TMEM columns, FP32)
 constexpr int BK = 64;           // K per stage (128 bytes of BF16 per row)
 constexpr int NTH = 128;         // 4 warps: warp w reads TMEM lanes 32w..32w+31
-constexpr int STAGES = 2;
+// stage ring of the asynchronous path (K blocks staged ahead of the MMAs)
+// and of the gather path
+constexpr int STAGES_ASYNC = 4, AHEAD_ASYNC = 2;
+constexpr int STAGES_GATHER = 2, AHEAD_GATHER = 0;
 constexpr int A_BYTES = BM * BK * 2;
 constexpr int B_BYTES = BN * BK * 2;
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 128;  // + alignment slack
-static_assert(BM * (BN + 1) * 4 <= STAGES * STAGE_BYTES, "epilogue tile must fit the stages");
+constexpr int smem_bytes(int stages) { return stages * STAGE_BYTES + 128; }  // + alignment slack
+static_assert(BM * (BN + 1) * 4 <= STAGES_GATHER * STAGE_BYTES, "epilogue tile must fit the stages");
 constexpr int TMEM_COLS = 64;    // power of two >= 32
 constexpr uint32_t LBO = 128;    // K-direction core-matrix stride (bytes)
 constexpr uint32_t SBO = 1024;   // M/N-direction 8-row-group stride (bytes)
@@ -62,8 +70,11 @@ struct gemm_params {
     int32_t m, n, nseg, ktotal;
     int32_t kstart[4];
     seg_t seg[3];
+    int32_t async_ok;  // every operand BF16, K contiguous, 16-byte aligned rows
     void* c;
     int64_t c_sm, c_sn, c_sz;
+    void* c2;          // optional second (BF16) copy of C with its own strides
+    int64_t c2_sm, c2_sn, c2_sz;
     int32_t c_type, mode, act;
     int32_t kblocks_per_split;
     float alpha;
@@ -232,6 +243,57 @@ __device__ __forceinline__ void gather_chunk(
     }
 }
 
+// 16 bytes global -> shared, asynchronous, L2 only; src_bytes 0 fills zeros
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template<int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// the 16-byte chunk (k0 .. k0+7) of row `row` of operand A (is_a) or B, copied
+// asynchronously to dst (zeros outside the operand); async_ok products only
+__device__ __forceinline__ void async_chunk(
+    const gemm_params& p, bool is_a, int z, int row, int rows, int k0, uint32_t dst)
+{
+    const void* src = is_a ? p.seg[0].a : p.seg[0].b;  // any valid address for a zero fill
+    uint32_t bytes = 0;
+    if (row < rows && k0 < p.ktotal) {
+        int s = 0;
+        if (p.nseg > 1 && k0 >= p.kstart[1]) s = 1;
+        if (p.nseg > 2 && k0 >= p.kstart[2]) s = 2;
+        const seg_t& g = p.seg[s];
+        const int64_t kl = k0 - p.kstart[s];
+        const int64_t off = is_a ? (int64_t) z * g.a_sz + (int64_t) row * g.a_sm + kl
+                                 : (int64_t) z * g.b_sz + (int64_t) row * g.b_sn + kl;
+        src = reinterpret_cast<const __nv_bfloat16*>(is_a ? g.a : g.b) + off;
+        const int nv = min(8, (int) (g.k - kl));
+        bytes = (uint32_t) nv * 2u;
+    }
+    cp_async16(dst, src, bytes);
+}
+
+// the A and B tiles of K block kb by asynchronous copies (async_ok products)
+__device__ __forceinline__ void async_stage(
+    const gemm_params& p, int z, int m0, int n0, int kb, uint32_t sa, uint32_t sb)
+{
+    const int k0 = kb * BK;
+    // K chunks first: a warp's 32 copies cover four rows of 128 contiguous bytes
+#pragma unroll
+    for (int i = 0; i < BM * (BK / 8) / NTH; i++) {
+        const int c = threadIdx.x + i * NTH, row = c >> 3, kc = c & 7;
+        async_chunk(p, true, z, m0 + row, p.m, k0 + kc * 8, sa + (uint32_t) (((row >> 3) * (BK / 8) + kc) * 128 +
+                                                                                 (row & 7) * 16));
+    }
+#pragma unroll
+    for (int i = 0; i < BN * (BK / 8) / NTH; i++) {
+        const int c = threadIdx.x + i * NTH, row = c >> 3, kc = c & 7;
+        async_chunk(p, false, z, n0 + row, p.n, k0 + kc * 8, sb + (uint32_t) (((row >> 3) * (BK / 8) + kc) * 128 +
+                                                                                  (row & 7) * 16));
+    }
+}
+
 // one 16-byte row of a core matrix, as BF16
 __device__ __forceinline__ void store_chunk(uint32_t dst, const float (&v)[8])
 {
@@ -302,6 +364,7 @@ __device__ __forceinline__ void load_stage(
     }
 }
 
+template<int STAGES, int AHEAD>
 __global__ void __launch_bounds__(NTH) gemm_kernel(const gemm_params p)
 {
     extern __shared__ __align__(128) uint8_t smem_raw[];
@@ -338,21 +401,42 @@ __global__ void __launch_bounds__(NTH) gemm_kernel(const gemm_params p)
     fence_after();
     const uint32_t tmem = tmem_sh;
 
+    // stage block j: asynchronously where every operand allows it, else by
+    // plain loads (complete when the call returns)
+    auto stage = [&](int j) {
+        const uint32_t sa = base + (uint32_t) ((j % STAGES) * STAGE_BYTES);
+        if (AHEAD > 0)  // only the asynchronous instantiation stages ahead
+            async_stage(p, z, m0, n0, kb0 + j, sa, sa + (uint32_t) A_BYTES);
+        else
+            load_stage(p, z, m0, n0, kb0 + j, sa, sa + (uint32_t) A_BYTES);
+    };
+    // exactly AHEAD copy groups before the loop (empty ones when there are
+    // fewer blocks), so that waiting for all but the AHEAD most recent groups
+    // in iteration it always covers block it
+    for (int j = 0; j < AHEAD; j++) {
+        if (j < nit) stage(j);
+        cp_async_commit();
+    }
     for (int it = 0; it < nit; it++) {
         const int st = it % STAGES;
-        const uint32_t sa = base + (uint32_t) (st * STAGE_BYTES);
-        const uint32_t sb = sa + (uint32_t) A_BYTES;
-        if (it >= STAGES) {
-            // the MMAs that read this stage two blocks ago must be done
-            if (!mbar_wait(mb0 + 8u * st, (uint32_t) (((it - STAGES) / STAGES) & 1))) fail_sh = 1;
+        const int ahead = it + AHEAD;
+        bool ok_wait = true;
+        if (ahead < nit) {
+            // the MMAs that read this stage STAGES blocks ago must be done
+            if (ahead >= STAGES)
+                ok_wait = mbar_wait(mb0 + 8u * (ahead % STAGES), (uint32_t) (((ahead - STAGES) / STAGES) & 1));
+            if (ok_wait) stage(ahead);
         }
-        __syncthreads();
-        if (fail_sh) break;
-        load_stage(p, z, m0, n0, kb0 + it, sa, sb);
+        if (!ok_wait) fail_sh = 1;
+        cp_async_commit();
+        cp_async_wait<AHEAD>();  // block it has landed (this thread's copies)
         fence_async_smem();
         __syncthreads();
+        if (fail_sh) break;
         if (tid == 0) {
             fence_after();
+            const uint32_t sa = base + (uint32_t) (st * STAGE_BYTES);
+            const uint32_t sb = sa + (uint32_t) A_BYTES;
 #pragma unroll
             for (int kk = 0; kk < BK / 16; kk++) {
                 const uint64_t ad = smem_desc(sa + (uint32_t) (kk * 256));
@@ -362,6 +446,7 @@ __global__ void __launch_bounds__(NTH) gemm_kernel(const gemm_params p)
             mma_commit(mb0 + 8u * st);
         }
     }
+    cp_async_wait<0>();  // no copy outlives the loop (a break leaves some in flight)
 
     bool ok = !fail_sh && nit > 0;
     if (ok) {
@@ -413,6 +498,24 @@ __global__ void __launch_bounds__(NTH) gemm_kernel(const gemm_params p)
                 reinterpret_cast<__nv_bfloat16*>(p.c)[off] = __float2bfloat16_rn(v);
             else
                 reinterpret_cast<float*>(p.c)[off] = v;
+        }
+        if (p.c2) {
+            // the same values (STORE mode) as BF16 in a second layout, e.g.
+            // the transposed copy the next product reads with K contiguous;
+            // written along its own contiguous dimension
+            const bool rows_fast2 = p.c2_sn != 1 && p.c2_sm == 1;
+#pragma unroll 1
+            for (int e = tid; e < BM * BN; e += NTH) {
+                const int r = rows_fast2 ? e % BM : e / BN;
+                const int cc = rows_fast2 ? e / BM : e % BN;
+                const int row = m0 + r, col = n0 + cc;
+                if (row >= p.m || col >= p.n) continue;
+                float v = p.alpha * tile[r * LD + cc];
+                if (p.bias) v += p.bias[col];
+                if (p.act == MBG_ACT_GELU) v = gelu(v);
+                const int64_t off = (int64_t) z * p.c2_sz + (int64_t) row * p.c2_sm + (int64_t) col * p.c2_sn;
+                reinterpret_cast<__nv_bfloat16*>(p.c2)[off] = __float2bfloat16_rn(v);
+            }
         }
     }
     if (fail_sh && tid == 0) atomicOr(p.status, ST_WAIT);
@@ -617,6 +720,24 @@ void gemm(const mbg_gemm_desc* d, cudaStream_t s)
     }
     p.kstart[d->nseg] = kt;
     p.ktotal = kt;
+    // asynchronous 16-byte copies need BF16 operands with K contiguous and
+    // every row (and batch) start on a 16-byte boundary, and no negation
+    bool async_ok = true;
+    for (int i = 0; i < d->nseg; i++) {
+        const mbg_gemm_segment& g = d->seg[i];
+        const bool ok = g.a_type == MBG_BF16 && g.b_type == MBG_BF16 && g.a_sk == 1 && g.b_sk == 1 &&
+            g.a_sm % 8 == 0 && g.b_sn % 8 == 0 && g.a_sz % 8 == 0 && g.b_sz % 8 == 0 &&
+            (reinterpret_cast<uintptr_t>(g.a) & 15) == 0 && (reinterpret_cast<uintptr_t>(g.b) & 15) == 0 &&
+            !g.negate && (i == d->nseg - 1 || g.k % 8 == 0);
+        async_ok = async_ok && ok;
+    }
+    p.async_ok = async_ok ? 1 : 0;
+    require(!d->c2 || (d->mode == MBG_GEMM_STORE && d->act != MBG_ACT_GELU_BWD),
+            "gemm: a second output needs STORE mode (no GELU_BWD)");
+    p.c2 = d->c2;
+    p.c2_sm = d->c2_sm;
+    p.c2_sn = d->c2_sn;
+    p.c2_sz = d->c2_sz;
     p.c = d->c;
     p.c_sm = d->c_sm;
     p.c_sn = d->c_sn;
@@ -637,8 +758,17 @@ void gemm(const mbg_gemm_desc* d, cudaStream_t s)
     const int64_t tiles = (int64_t) ((d->m + BM - 1) / BM) * ((d->n + BN - 1) / BN);
     require(tiles <= 0x7fffffff, "gemm: too many tiles");
     static std::once_flag attr;
-    std::call_once(attr, [] { cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES); });
-    gemm_kernel<<<dim3((unsigned) tiles, (unsigned) ysplits, (unsigned) d->batch), NTH, SMEM_BYTES, s>>>(p);
+    std::call_once(attr, [] {
+        cudaFuncSetAttribute(gemm_kernel<STAGES_ASYNC, AHEAD_ASYNC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem_bytes(STAGES_ASYNC));
+        cudaFuncSetAttribute(gemm_kernel<STAGES_GATHER, AHEAD_GATHER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem_bytes(STAGES_GATHER));
+    });
+    const dim3 grid((unsigned) tiles, (unsigned) ysplits, (unsigned) d->batch);
+    if (p.async_ok)
+        gemm_kernel<STAGES_ASYNC, AHEAD_ASYNC><<<grid, NTH, smem_bytes(STAGES_ASYNC), s>>>(p);
+    else
+        gemm_kernel<STAGES_GATHER, AHEAD_GATHER><<<grid, NTH, smem_bytes(STAGES_GATHER), s>>>(p);
     check_launch("gemm_kernel");
 }
 

@@ -263,12 +263,13 @@ def train(net, X, Y, epochs=20, batch=64, lr=2e-3, seed=0, weight_decay=1e-4,
     return hist
 
 
-def predict(net, X, batch=256):
-    """Surrogate outputs [n, S] for inputs X (FP32 [n, S, F])."""
+def predict(net, X, batch=1024):
+    """Surrogate outputs [n, S] for inputs X (FP32 [n, S, F]), through the
+    network's inference path (FNO.infer)."""
     out = torch.empty(X.shape[0], X.shape[1], dtype=torch.float32, device=X.device)
     for i in range(0, X.shape[0], batch):
         xb = X[i:i + batch]
-        out[i:i + xb.shape[0]] = net.forward(xb)
+        out[i:i + xb.shape[0]] = net.infer(xb)
     return out
 
 
@@ -334,10 +335,10 @@ solver's lower quartile on the judged points). Returns a report dict."""
 
     p_sw = space.sample(n_sweep, seed=seed + 2)
     X_sw = space.features(p_sw)
-    predict(net, X_sw[:batch * 4], batch=batch * 4)     # warm-up
+    predict(net, X_sw[:1024], batch=1024)     # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    pred = predict(net, X_sw, batch=256)
+    pred = predict(net, X_sw, batch=1024)
     torch.cuda.synchronize()
     t_sur = time.perf_counter() - t0
     nj = n_sweep if n_judge is None else min(n_judge, n_sweep)

@@ -111,7 +111,9 @@ class FNO:
         self.blk = [torch.empty(sh.Mo * 4 * sh.W * sh.W, dtype=torch.bfloat16,
                                 device=self.dev) for _ in range(sh.L)]
         self._bufs = {}
+        self._ibufs = {}
         self._blk_valid = False
+        self._wb = {}   # BF16 copies of the dense weights (inference)
 
     # ------------------------------------------------------------ helpers
     def _views(self, flat):
@@ -154,6 +156,14 @@ class FNO:
         for l in range(self.sh.L):
             K.mode_blocks(self.p["wr%d" % l].view(self.sh.Mo, self.sh.W, self.sh.W),
                           self.p["wi%d" % l], self.blk[l])
+        # BF16 copies of the dense weights for infer() (the same rounding the
+        # products apply to the FP32 weights when they load them)
+        for name in ["W%d" % l for l in range(self.sh.L)] + ["Q1", "q2"]:
+            w = self._wb.get(name)
+            if w is None:
+                w = self._wb[name] = torch.empty(self.p[name].numel(), dtype=torch.bfloat16,
+                                                 device=self.dev)
+            K.cast_bf16(self.p[name], w)
         self._blk_valid = True
 
     @staticmethod
@@ -210,6 +220,84 @@ class FNO:
         K.gemm(B * S, Hq, [Seg(b["v"][L], 0, W, 1, 0, p["Q1"], 0, W, 1, 0, W)],
                b["h"], 0, Hq, 1, bias=p["bq1"], act=T.MBG_ACT_GELU, pre=b["ph"])
         K.gemm(B * S, 1, [Seg(b["h"], 0, Hq, 1, 0, p["q2"], 0, 0, 1, 0, Hq)],
+               b["y"], 0, 1, 1, bias=p["bq2"])
+        return b["y"].view(B, S)
+
+    def _ibuffers(self, B):
+        if B in self._ibufs:
+            return self._ibufs[B]
+        sh, d = self.sh, self.dev
+        S, W, Mo, Hq = sh.S, sh.W, sh.Mo, sh.Hq
+        b16 = torch.bfloat16
+        b = dict(
+            v=[torch.empty(B * S * W, dtype=b16, device=d) for _ in range(2)],
+            vT=[torch.empty(B * W * S, dtype=b16, device=d) for _ in range(2)],
+            Vh=torch.empty(B * W * 2 * Mo, dtype=torch.float32, device=d),
+            Y=torch.empty(B * W * 2 * Mo, dtype=b16, device=d),
+            h=torch.empty(B * S * Hq, dtype=b16, device=d),
+            y=torch.empty(B * S, dtype=torch.float32, device=d))
+        self._ibufs[B] = b
+        return b
+
+    def infer(self, X):
+        """The forward pass for inference (prescreening sweeps): the same
+        network and the same BF16 rounding of every product operand as
+        forward(), with the operands laid out so that every heavy product
+        reads BF16 with K contiguous (the GEMM then stages them by
+        asynchronous copies, four stages deep): each activation is kept as
+        [B, S, W] and, written by the same epilogue, as [B, W, S]; the mixed
+        spectrum as BF16 [B, W, 2 Mo]; BF16 copies of the dense weights. The
+        truncated DFT is then one product over all B W rows with K = S (no
+        split-K); no pre-activations are stored. X: FP32 [B, S, F]; returns
+        y [B, S] (a view of an internal buffer)."""
+        sh = self.sh
+        S, W, Mo, L, Fi, Hq = sh.S, sh.W, sh.Mo, sh.L, sh.F, sh.Hq
+        B = X.shape[0]
+        if tuple(X.shape) != (B, S, Fi) or X.dtype != torch.float32:
+            raise ValueError("X must be FP32 [B, %d, %d]" % (S, Fi))
+        X = X.contiguous()
+        b = self._ibuffers(B)
+        p = self.p
+        if not self._blk_valid:
+            self._mode_blocks()
+        wb = self._wb
+        # lifting, per sample: v0[b] = X[b] P^T + bp, also as vT0[b] [W, S]
+        K.gemm(S, W, [Seg(X, 0, Fi, 1, S * Fi, p["P"], 0, Fi, 1, 0, Fi)],
+               b["v"][0], 0, W, 1, S * W, batch=B, bias=p["bp"],
+               c2=b["vT"][0], c2_sm=1, c2_sn=S, c2_sz=W * S)
+        cur = 0
+        for l in range(L):
+            v, vT = b["v"][cur], b["vT"][cur]
+            vh, Y = b["Vh"], b["Y"]
+            # truncated DFT over all B W rows: Vh[(b, c), m'] = vT[(b, c), :] F[m', :]
+            K.gemm(B * W, 2 * Mo, [Seg(vT, 0, S, 1, 0, self.F, 0, S, 1, 0, S)],
+                   vh, 0, 2 * Mo, 1)
+            # mode mixing per mode m, the Re and the Im outputs into
+            # Y[b, o, m] and Y[b, o, Mo + m] (BF16)
+            blk = self.blk[l]
+            for part in range(2):
+                K.gemm(B, W,
+                       [Seg(vh, 0, W * 2 * Mo, 2 * Mo, 1, blk, part * W * 2 * W,
+                            2 * W, 1, 4 * W * W, W),
+                        Seg(vh, Mo, W * 2 * Mo, 2 * Mo, 1, blk,
+                            part * W * 2 * W + W, 2 * W, 1, 4 * W * W, W)],
+                       Y, part * Mo, W * 2 * Mo, 2 * Mo, 1, batch=Mo)
+            # inverse DFT + pointwise path + bias (+ GELU), per sample,
+            # written as [S, W] and as [W, S]
+            last = l == L - 1
+            nxt = 1 - cur
+            K.gemm(S, W,
+                   [Seg(self.G, 0, 2 * Mo, 1, 0, Y, 0, 2 * Mo, 1, W * 2 * Mo, 2 * Mo),
+                    Seg(v, 0, W, 1, S * W, wb["W%d" % l], 0, W, 1, 0, W)],
+                   b["v"][nxt], 0, W, 1, S * W, batch=B, bias=p["bw%d" % l],
+                   act=T.MBG_ACT_NONE if last else T.MBG_ACT_GELU,
+                   c2=None if last else b["vT"][nxt], c2_sm=1, c2_sn=S,
+                   c2_sz=W * S)
+            cur = nxt
+        # projection
+        K.gemm(B * S, Hq, [Seg(b["v"][cur], 0, W, 1, 0, wb["Q1"], 0, W, 1, 0, W)],
+               b["h"], 0, Hq, 1, bias=p["bq1"], act=T.MBG_ACT_GELU)
+        K.gemm(B * S, 1, [Seg(b["h"], 0, Hq, 1, 0, wb["q2"], 0, 0, 1, 0, Hq)],
                b["y"], 0, 1, 1, bias=p["bq2"])
         return b["y"].view(B, S)
 
@@ -347,11 +435,19 @@ def main(argv=None):
         net.forward(X)
     torch.cuda.synchronize()
     dt_fwd = (time.perf_counter() - t0) / a.steps
+    net.infer(X)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        net.infer(X)
+    torch.cuda.synchronize()
+    dt_inf = (time.perf_counter() - t0) / a.steps
     print(json.dumps({"shapes": vars(sh), "batch": a.batch,
                       "train_step_ms": dt_train * 1e3,
-                      "forward_ms": dt_fwd * 1e3,
+                      "forward_ms": dt_fwd * 1e3, "infer_ms": dt_inf * 1e3,
                       "samples_per_s_train": a.batch / dt_train,
                       "samples_per_s_forward": a.batch / dt_fwd,
+                      "samples_per_s_infer": a.batch / dt_inf,
                       "loss": float(loss.item()), "status": K.status()}))
 
 

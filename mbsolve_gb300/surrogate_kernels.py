@@ -61,9 +61,10 @@ class Seg:
 
 def gemm(m, n, segs, c, c_off, c_sm, c_sn, c_sz=0, batch=1,
          mode=T.MBG_GEMM_STORE, act=T.MBG_ACT_NONE, alpha=1.0, bias=None,
-         pre=None, gate=None, split_k=1):
+         pre=None, gate=None, split_k=1, c2=None, c2_sm=0, c2_sn=0, c2_sz=0):
     """C[z](i, j) = epilogue(alpha sum_s sum_k A_s(i, k) B_s(j, k)) for
-    i < m, j < n, z < batch, on the tensor cores (BF16 x BF16 -> FP32)."""
+    i < m, j < n, z < batch, on the tensor cores (BF16 x BF16 -> FP32);
+    c2 (BF16, STORE mode): the same values again with strides c2_*."""
     d = T.mbg_gemm_desc()
     d.m, d.n, d.batch, d.nseg = int(m), int(n), int(batch), len(segs)
     if not 1 <= len(segs) <= 3:
@@ -98,6 +99,12 @@ def gemm(m, n, segs, c, c_off, c_sm, c_sn, c_sz=0, batch=1,
     d.bias = _ptr(bias) if bias is not None else None
     d.pre = _ptr(pre, c_off) if pre is not None else None
     d.gate = _ptr(gate, c_off) if gate is not None else None
+    if c2 is not None:
+        if c2.dtype != torch.bfloat16:
+            raise ValueError("gemm c2: BF16 only")
+        _check_span(c2, 0, [(batch, c2_sz), (m, c2_sm), (n, c2_sn)], "gemm c2")
+        d.c2 = _ptr(c2)
+        d.c2_sm, d.c2_sn, d.c2_sz = c2_sm, c2_sn, c2_sz
     _native.check(_lib().mbg_fno_gemm(C.byref(d), _stream()))
 
 

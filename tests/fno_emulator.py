@@ -17,7 +17,8 @@ def _bf(x):
 
 
 def gemm(m, n, segs, c, c_off, c_sm, c_sn, c_sz=0, batch=1, mode=0, act=0,
-         alpha=1.0, bias=None, pre=None, gate=None, split_k=1):
+         alpha=1.0, bias=None, pre=None, gate=None, split_k=1, c2=None,
+         c2_sm=0, c2_sn=0, c2_sz=0):
     acc = torch.zeros(batch, m, n, dtype=torch.float64)
     for s in segs:
         A = _bf(_view(s.a, s.a_off, (batch, m, s.k), (s.a_sz, s.a_sm, s.a_sk)))
@@ -44,6 +45,12 @@ def gemm(m, n, segs, c, c_off, c_sm, c_sn, c_sz=0, batch=1, mode=0, act=0,
         v = v * (0.5 * (1.0 + torch.erf(g / math.sqrt(2.0))) +
                  g * torch.exp(-0.5 * g * g) / math.sqrt(2.0 * math.pi))
     C.copy_(v.to(C.dtype))
+    if c2 is not None:
+        _view(c2, 0, (batch, m, n), (c2_sz, c2_sm, c2_sn)).copy_(v.to(c2.dtype))
+
+
+def cast_bf16(x, y):
+    y.copy_(x.reshape(-1)[:y.numel()].to(torch.bfloat16))
 
 
 def mode_blocks(wr, wi, blk):
@@ -78,5 +85,5 @@ def adam(w, g, m, v, lr, beta1, beta2, eps, weight_decay, step):
 def install(monkeypatch):
     """Route the surrogate module's kernel calls to this model."""
     from mbsolve_gb300 import surrogate as S
-    for name in ("gemm", "mode_blocks", "colsum", "mse", "adam"):
+    for name in ("gemm", "mode_blocks", "colsum", "mse", "adam", "cast_bf16"):
         monkeypatch.setattr(S.K, name, globals()[name])

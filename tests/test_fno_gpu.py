@@ -133,3 +133,29 @@ def test_training_fits_a_pulse_operator(S):
     last = np.mean([net.train_step(Xg[i:i + B], Tg[i:i + B], lr=1e-3).item()
                     for i in range(0, N, B)])
     assert last < first / 20, (first, last)
+
+
+@pytest.mark.parametrize("args,B", [(dict(S=128, W=16, Mo=8, L=2, F=8, Hq=32), 16),
+                                    ({}, 24)])
+def test_inference_path_matches_forward_and_oracle(S, args, B):
+    """FNO.infer (BF16 operands with K contiguous, staged by asynchronous
+    copies; the DFT as one product without split-K) equals forward() and
+    the oracle's bf16-mode output; two calls in a row give the same."""
+    sh = S.Shapes(**args)
+    net = S.FNO(sh, seed=5)
+    rng = np.random.default_rng(12)
+    X = torch.tensor(rng.normal(size=(B, sh.S, sh.F)).astype(np.float32),
+                     device="cuda")
+    yf = net.forward(X).clone()
+    yi = net.infer(X).clone()
+    yi2 = net.infer(X).clone()
+    torch.cuda.synchronize()
+    from mbsolve_gb300 import surrogate_kernels as K
+    assert K.status() == 0
+    assert torch.equal(yi, yi2)
+    assert _rel(yi.cpu().numpy(), yf.cpu().numpy()) <= 2e-3
+    _, _, y_o = O.forward_backward(O.Shapes(**args), net.theta.cpu().double().numpy(),
+                                   X.cpu().double().numpy(),
+                                   np.zeros((B, sh.S)), bf16=True)
+    assert _rel(yi.cpu().numpy(), y_o) <= TOL_Y
+

@@ -82,3 +82,20 @@ def test_sweep_space_is_deterministic():
     assert float(X[..., 1:8].abs().max()) <= 1.0 + 1e-6
     dev, sce = a.run(pa, 0)
     assert sce.get_num_gridpoints() == a.n_x
+
+
+def test_inference_plan_equals_forward(monkeypatch):
+    """FNO.infer's products (K-contiguous BF16 layouts, the transposed
+    activation copies, the mixed spectrum as [B, W, 2 Mo], BF16 weight
+    copies) compute the same network as forward(), through the CPU model
+    of the kernels."""
+    from mbsolve_gb300 import surrogate as S
+    E.install(monkeypatch)
+    sh = S.Shapes(S=64, W=16, Mo=8, L=3, F=5, Hq=24)
+    net = S.FNO(sh, seed=2, device="cpu")
+    X = torch.tensor(np.random.default_rng(4).normal(size=(3, 64, 5)),
+                     dtype=torch.float32)
+    yf = net.forward(X).clone().double().numpy()
+    yi = net.infer(X).clone().double().numpy()
+    assert np.linalg.norm(yi - yf) <= 1e-6 * np.linalg.norm(yf)
+
