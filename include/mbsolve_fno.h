@@ -82,12 +82,20 @@ typedef struct mbg_gemm_desc {
     const float* bias;
     float* pre;
     const float* gate;
-    /* optional second output (NULL: none; STORE mode only): the same
-     * values as BF16 at c2 + z c2_sz + i c2_sm + j c2_sn, e.g. the
-     * transposed copy of an activation that the next product reads with
-     * K contiguous */
+    /* optional second output (NULL: none; STORE mode without pre, gate
+     * or GELU_BWD): the same values as BF16 at
+     * c2 + z c2_sz + i c2_sm + j c2_sn, e.g. the transposed copy of an
+     * activation that the next product reads with K contiguous */
     void* c2;
     int64_t c2_sm, c2_sn, c2_sz;
+    /* optional (NULL: none; STORE mode without pre, gate or GELU_BWD, an
+     * FP32 C, no second output): instead of storing the outputs v(i, j),
+     * add sum_j rowdot[j] v(i, j) (both rounded to BF16) to C[z](i, 0),
+     * atomically, plus *rowdot_bias once (when not NULL): a following
+     * product with one output column folded into this one's epilogue.
+     * C must hold the starting values (e.g. zeros). */
+    const float* rowdot;
+    const float* rowdot_bias;
 } mbg_gemm_desc;
 
 int mbg_fno_gemm(const mbg_gemm_desc* d, void* stream);

@@ -190,4 +190,5 @@ class mbg_gemm_desc(C.Structure):
         ("gate", C.c_void_p),
         ("c2", C.c_void_p),
         ("c2_sm", C.c_int64), ("c2_sn", C.c_int64), ("c2_sz", C.c_int64),
+        ("rowdot", C.c_void_p), ("rowdot_bias", C.c_void_p),
     ]

@@ -43,8 +43,11 @@ constexpr int BN = 64;           // columns of a tile (TMEM columns, FP32)
 constexpr int BK = 64;           // K per stage (128 bytes of BF16 per row)
 constexpr int NTH = 128;         // 4 warps: warp w reads TMEM lanes 32w..32w+31
 // stage ring of the asynchronous path (K blocks staged ahead of the MMAs)
-// and of the gather path
+// and of the gather path; products of at most two K blocks (per split)
+// take an asynchronous two-stage ring (half the shared memory: twice the
+// CTAs per SM)
 constexpr int STAGES_ASYNC = 4, AHEAD_ASYNC = 2;
+constexpr int STAGES_SHORT = 2, AHEAD_SHORT = 2;
 constexpr int STAGES_GATHER = 2, AHEAD_GATHER = 0;
 constexpr int A_BYTES = BM * BK * 2;
 constexpr int B_BYTES = BN * BK * 2;
@@ -71,10 +74,16 @@ struct gemm_params {
     int32_t kstart[4];
     seg_t seg[3];
     int32_t async_ok;  // every operand BF16, K contiguous, 16-byte aligned rows
+    int32_t vec_c;     // STORE epilogue as 16-byte stores of 8 outputs along C's rows
+    int32_t vec_c2;    // the second output as 16-byte stores of 8 outputs along its columns
+    int32_t fin;       // STORE mode without pre or gate: bias and activation applied once, on
+                       // the way from TMEM into the shared tile
     void* c;
     int64_t c_sm, c_sn, c_sz;
     void* c2;          // optional second (BF16) copy of C with its own strides
     int64_t c2_sm, c2_sn, c2_sz;
+    const float* rowdot;       // optional: C(i) += sum_j rowdot[j] out(i, j) instead of storing out
+    const float* rowdot_bias;
     int32_t c_type, mode, act;
     int32_t kblocks_per_split;
     float alpha;
@@ -470,18 +479,86 @@ __global__ void __launch_bounds__(NTH) gemm_kernel(const gemm_params p)
         for (int cb = 0; cb < BN / 16; cb++) {
             float acc[16];
             tmem_ld16(tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) (cb * 16), acc);
+            if (p.fin) {
+#pragma unroll
+                for (int i = 0; i < 16; i++) {
+                    const int col = n0 + cb * 16 + i;
+                    float v = p.alpha * acc[i];
+                    if (p.bias && col < p.n) v += p.bias[col];
+                    if (p.act == MBG_ACT_GELU) v = gelu(v);
+                    acc[i] = v;
+                }
+            }
 #pragma unroll
             for (int i = 0; i < 16; i++) tile[r0 * LD + cb * 16 + i] = acc[i];
         }
         __syncthreads();
+        // final value of tile entry (r, cc) in STORE mode without pre or gate
+        auto value = [&](int r, int cc) { return tile[r * LD + cc]; };
         const bool rows_fast = p.c_sn != 1 && p.c_sm == 1;
+        if (p.rowdot) {
+            // a second product folded into the epilogue: each row's outputs
+            // dotted with rowdot (both rounded to BF16, as a product's
+            // operands), one atomic add per row and tile into the FP32
+            // vector C (the first column tile adds rowdot_bias)
+            const int row = m0 + tid;
+            if (row < p.m) {
+                float s = (n0 == 0 && p.rowdot_bias) ? *p.rowdot_bias : 0.0f;
+                for (int cc = 0; cc < BN && n0 + cc < p.n; cc++) {
+                    const float a = __bfloat162float(__float2bfloat16_rn(value(tid, cc)));
+                    const float w = __bfloat162float(__float2bfloat16_rn(p.rowdot[n0 + cc]));
+                    s = fmaf(a, w, s);
+                }
+                atomicAdd(reinterpret_cast<float*>(p.c) + (int64_t) z * p.c_sz + (int64_t) row * p.c_sm, s);
+            }
+        } else if (p.vec_c) {
+            // 8 consecutive outputs of a row per 16-byte (BF16) or 2 x 16-byte
+            // (FP32) store; a warp writes four rows of 64 outputs
 #pragma unroll 1
-        for (int e = tid; e < BM * BN; e += NTH) {
+            for (int e = tid; e < BM * (BN / 8); e += NTH) {
+                const int r = e >> 3, c0 = (e & 7) * 8;
+                const int row = m0 + r, col0 = n0 + c0;
+                if (row >= p.m || col0 >= p.n) continue;
+                const int64_t off = (int64_t) z * p.c_sz + (int64_t) row * p.c_sm + col0;
+                if (col0 + 8 <= p.n) {
+                    float v[8];
+#pragma unroll
+                    for (int i = 0; i < 8; i++) v[i] = value(r, c0 + i);
+                    if (p.c_type == MBG_BF16) {
+                        const uint4 q = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]),
+                                                   pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
+                        *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(p.c) + off) = q;
+                    } else {
+                        float4* d4 = reinterpret_cast<float4*>(reinterpret_cast<float*>(p.c) + off);
+                        d4[0] = make_float4(v[0], v[1], v[2], v[3]);
+                        d4[1] = make_float4(v[4], v[5], v[6], v[7]);
+                    }
+                } else {
+                    for (int i = 0; col0 + i < p.n; i++) {
+                        const float v = value(r, c0 + i);
+                        if (p.c_type == MBG_BF16)
+                            reinterpret_cast<__nv_bfloat16*>(p.c)[off + i] = __float2bfloat16_rn(v);
+                        else
+                            reinterpret_cast<float*>(p.c)[off + i] = v;
+                    }
+                }
+            }
+        }
+#pragma unroll 1
+        for (int e = (p.vec_c || p.rowdot) ? BM * BN : tid; e < BM * BN; e += NTH) {
             const int r = rows_fast ? e % BM : e / BN;
             const int cc = rows_fast ? e / BM : e % BN;
             const int row = m0 + r, col = n0 + cc;
             if (row >= p.m || col >= p.n) continue;
             const int64_t off = (int64_t) z * p.c_sz + (int64_t) row * p.c_sm + (int64_t) col * p.c_sn;
+            if (p.fin) {
+                const float v = tile[r * LD + cc];
+                if (p.c_type == MBG_BF16)
+                    reinterpret_cast<__nv_bfloat16*>(p.c)[off] = __float2bfloat16_rn(v);
+                else
+                    reinterpret_cast<float*>(p.c)[off] = v;
+                continue;
+            }
             float v = p.alpha * tile[r * LD + cc];
             if (p.mode == MBG_GEMM_ATOMIC) {
                 atomicAdd(reinterpret_cast<float*>(p.c) + off, v);
@@ -499,9 +576,31 @@ __global__ void __launch_bounds__(NTH) gemm_kernel(const gemm_params p)
             else
                 reinterpret_cast<float*>(p.c)[off] = v;
         }
-        if (p.c2) {
-            // the same values (STORE mode) as BF16 in a second layout, e.g.
-            // the transposed copy the next product reads with K contiguous;
+        if (p.c2 && p.vec_c2) {
+            // the same values (STORE mode) as BF16 in a second layout whose
+            // rows are contiguous (e.g. the transposed copy the next product
+            // reads with K contiguous): 8 rows of a column per 16-byte store,
+            // a warp writes two columns of 128 rows
+#pragma unroll 1
+            for (int e = tid; e < BM * BN / 8; e += NTH) {
+                const int rc = e & (BM / 8 - 1), cc = e / (BM / 8);
+                const int r0 = rc * 8, row0 = m0 + r0, col = n0 + cc;
+                if (row0 >= p.m || col >= p.n) continue;
+                const int64_t off = (int64_t) z * p.c2_sz + row0 + (int64_t) col * p.c2_sn;
+                if (row0 + 8 <= p.m) {
+                    float v[8];
+#pragma unroll
+                    for (int i = 0; i < 8; i++) v[i] = value(r0 + i, cc);
+                    const uint4 q = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]),
+                                               pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
+                    *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(p.c2) + off) = q;
+                } else {
+                    for (int i = 0; row0 + i < p.m; i++)
+                        reinterpret_cast<__nv_bfloat16*>(p.c2)[off + i] = __float2bfloat16_rn(value(r0 + i, cc));
+                }
+            }
+        } else if (p.c2) {
+            // the same values (STORE mode) as BF16 in a second layout,
             // written along its own contiguous dimension
             const bool rows_fast2 = p.c2_sn != 1 && p.c2_sm == 1;
 #pragma unroll 1
@@ -510,9 +609,7 @@ __global__ void __launch_bounds__(NTH) gemm_kernel(const gemm_params p)
                 const int cc = rows_fast2 ? e / BM : e % BN;
                 const int row = m0 + r, col = n0 + cc;
                 if (row >= p.m || col >= p.n) continue;
-                float v = p.alpha * tile[r * LD + cc];
-                if (p.bias) v += p.bias[col];
-                if (p.act == MBG_ACT_GELU) v = gelu(v);
+                const float v = value(r, cc);
                 const int64_t off = (int64_t) z * p.c2_sz + (int64_t) row * p.c2_sm + (int64_t) col * p.c2_sn;
                 reinterpret_cast<__nv_bfloat16*>(p.c2)[off] = __float2bfloat16_rn(v);
             }
@@ -732,12 +829,27 @@ void gemm(const mbg_gemm_desc* d, cudaStream_t s)
         async_ok = async_ok && ok;
     }
     p.async_ok = async_ok ? 1 : 0;
-    require(!d->c2 || (d->mode == MBG_GEMM_STORE && d->act != MBG_ACT_GELU_BWD),
-            "gemm: a second output needs STORE mode (no GELU_BWD)");
+    // STORE mode without pre-activation or gate: the finished values are
+    // computed once, into the shared tile, and may be stored twice
+    const bool plain_store = d->mode == MBG_GEMM_STORE && !d->pre && !d->gate && d->act != MBG_ACT_GELU_BWD;
+    require(!d->c2 || plain_store, "gemm: a second output needs STORE mode without pre, gate or GELU_BWD");
     p.c2 = d->c2;
     p.c2_sm = d->c2_sm;
     p.c2_sn = d->c2_sn;
     p.c2_sz = d->c2_sz;
+    // vectorised epilogues: the stored dimension contiguous, every 8-output
+    // chunk 16-byte aligned
+    const int64_t cw = d->c_type == MBG_BF16 ? 8 : 4;
+    p.vec_c = plain_store && d->c_sn == 1 && d->c_sm % cw == 0 && d->c_sz % cw == 0 &&
+        (reinterpret_cast<uintptr_t>(d->c) & 15) == 0;
+    p.vec_c2 = d->c2 && d->c2_sm == 1 && d->c2_sn % 8 == 0 && d->c2_sz % 8 == 0 &&
+        (reinterpret_cast<uintptr_t>(d->c2) & 15) == 0;
+    require(!d->rowdot || (plain_store && !d->c2 && d->c_type == MBG_F32 && d->act != MBG_ACT_GELU_BWD),
+            "gemm: rowdot needs STORE mode, an FP32 C and no second output");
+    p.rowdot = d->rowdot;
+    p.rowdot_bias = d->rowdot_bias;
+    if (p.rowdot) p.vec_c = 0;
+    p.fin = plain_store ? 1 : 0;
     p.c = d->c;
     p.c_sm = d->c_sm;
     p.c_sn = d->c_sn;
@@ -763,9 +875,15 @@ void gemm(const mbg_gemm_desc* d, cudaStream_t s)
                              smem_bytes(STAGES_ASYNC));
         cudaFuncSetAttribute(gemm_kernel<STAGES_GATHER, AHEAD_GATHER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              smem_bytes(STAGES_GATHER));
+        cudaFuncSetAttribute(gemm_kernel<STAGES_SHORT, AHEAD_SHORT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem_bytes(STAGES_SHORT));
     });
     const dim3 grid((unsigned) tiles, (unsigned) ysplits, (unsigned) d->batch);
-    if (p.async_ok)
+    // (with at most AHEAD_SHORT = STAGES_SHORT blocks every block is staged
+    // before the loop, so no stage is ever reused)
+    if (p.async_ok && p.kblocks_per_split <= STAGES_SHORT)
+        gemm_kernel<STAGES_SHORT, AHEAD_SHORT><<<grid, NTH, smem_bytes(STAGES_SHORT), s>>>(p);
+    else if (p.async_ok)
         gemm_kernel<STAGES_ASYNC, AHEAD_ASYNC><<<grid, NTH, smem_bytes(STAGES_ASYNC), s>>>(p);
     else
         gemm_kernel<STAGES_GATHER, AHEAD_GATHER><<<grid, NTH, smem_bytes(STAGES_GATHER), s>>>(p);

@@ -61,10 +61,13 @@ class Seg:
 
 def gemm(m, n, segs, c, c_off, c_sm, c_sn, c_sz=0, batch=1,
          mode=T.MBG_GEMM_STORE, act=T.MBG_ACT_NONE, alpha=1.0, bias=None,
-         pre=None, gate=None, split_k=1, c2=None, c2_sm=0, c2_sn=0, c2_sz=0):
+         pre=None, gate=None, split_k=1, c2=None, c2_sm=0, c2_sn=0, c2_sz=0,
+         rowdot=None, rowdot_bias=None):
     """C[z](i, j) = epilogue(alpha sum_s sum_k A_s(i, k) B_s(j, k)) for
     i < m, j < n, z < batch, on the tensor cores (BF16 x BF16 -> FP32);
-    c2 (BF16, STORE mode): the same values again with strides c2_*."""
+    c2 (BF16, STORE mode): the same values again with strides c2_*;
+    rowdot (FP32 [n]): C[z](i, 0) += rowdot . out(i, :) (+ rowdot_bias)
+    instead of storing out (FP32 C holding the starting values)."""
     d = T.mbg_gemm_desc()
     d.m, d.n, d.batch, d.nseg = int(m), int(n), int(batch), len(segs)
     if not 1 <= len(segs) <= 3:
@@ -105,6 +108,12 @@ def gemm(m, n, segs, c, c_off, c_sm, c_sn, c_sz=0, batch=1,
         _check_span(c2, 0, [(batch, c2_sz), (m, c2_sm), (n, c2_sn)], "gemm c2")
         d.c2 = _ptr(c2)
         d.c2_sm, d.c2_sn, d.c2_sz = c2_sm, c2_sn, c2_sz
+    if rowdot is not None:
+        if rowdot.dtype != torch.float32 or rowdot.numel() < n:
+            raise ValueError("gemm rowdot: FP32 with n entries")
+        d.rowdot = _ptr(rowdot)
+        if rowdot_bias is not None:
+            d.rowdot_bias = _ptr(rowdot_bias)
     _native.check(_lib().mbg_fno_gemm(C.byref(d), _stream()))
 
 

@@ -18,7 +18,7 @@ def _bf(x):
 
 def gemm(m, n, segs, c, c_off, c_sm, c_sn, c_sz=0, batch=1, mode=0, act=0,
          alpha=1.0, bias=None, pre=None, gate=None, split_k=1, c2=None,
-         c2_sm=0, c2_sn=0, c2_sz=0):
+         c2_sm=0, c2_sn=0, c2_sz=0, rowdot=None, rowdot_bias=None):
     acc = torch.zeros(batch, m, n, dtype=torch.float64)
     for s in segs:
         A = _bf(_view(s.a, s.a_off, (batch, m, s.k), (s.a_sz, s.a_sm, s.a_sk)))
@@ -36,6 +36,15 @@ def gemm(m, n, segs, c, c_off, c_sm, c_sn, c_sz=0, batch=1, mode=0, act=0,
     if bias is not None:
         v = v + bias[:n].to(torch.float64)
     v = v.to(torch.float32).to(torch.float64)
+    if rowdot is not None:
+        if act == 1:
+            v = 0.5 * v * (1.0 + torch.erf(v / math.sqrt(2.0)))
+        s = (_bf(v) * _bf(rowdot[:n].to(torch.float64))).sum(-1)
+        if rowdot_bias is not None:
+            s = s + rowdot_bias[0].to(torch.float64)
+        Cv = _view(c, c_off, (batch, m), (c_sz, c_sm))
+        Cv.copy_((Cv.to(torch.float64) + s).to(Cv.dtype))
+        return
     if pre is not None:
         _view(pre, c_off, (batch, m, n), (c_sz, c_sm, c_sn)).copy_(v.to(torch.float32))
     if act == 1:
