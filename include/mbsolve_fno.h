@@ -11,6 +11,10 @@
  *                      in tensor memory) over up to three strided operand
  *                      pairs, with bias / GELU / GELU-derivative epilogues,
  *                      accumulate and split-K atomic modes
+ *   mbg_fno_spectral_layer  one Fourier layer of inference in one launch:
+ *                      lifting or inverse DFT + pointwise mix, bias, GELU,
+ *                      then the next truncated DFT or the projection, the
+ *                      intermediate products kept on chip
  *   mbg_fno_mode_blocks  complex spectral weights -> real 2x2 block matrices
  *   mbg_fno_cast_bf16  FP32 -> BF16 copies of the master weights
  *   mbg_fno_colsum     bias gradients (column sums)
@@ -99,6 +103,54 @@ typedef struct mbg_gemm_desc {
 } mbg_gemm_desc;
 
 int mbg_fno_gemm(const mbg_gemm_desc* d, void* stream);
+
+enum {
+    MBG_LAYER_LIFT = 0,   /* lifting, then the first layer's truncated DFT */
+    MBG_LAYER_MID = 1,    /* inverse DFT + pointwise mix, then the next DFT */
+    MBG_LAYER_LAST = 2    /* inverse DFT + pointwise mix, then the projection */
+};
+
+/* One Fourier layer of inference for every sample in one launch, the
+ * layer's products kept on chip (one CTA per SM owns whole samples).
+ * Layouts, row-major, BF16 unless stated, all 16-byte aligned:
+ *   X [B][S][Fi] FP32, P [W][Fi] FP32        (LIFT)
+ *   v [B][S][W], Y [B][2][W][Mo] (Re then Im of the mixed spectrum),
+ *   G [S][2 Mo], Wl [W][W]                   (MID, LAST)
+ *   bias [W] FP32 (NULL: zero)
+ *   F [2 Mo][S], v_out [B][S][W], vhT [B][2 Mo][W]   (LIFT, MID)
+ *   Q1 [Hq][W], bq1 [Hq], q2 [Hq], bq2 [1] FP32, y [B][S] FP32   (LAST)
+ * Arithmetic: every product operand rounded to BF16, FP32 accumulation.
+ *   u(s, o) = sum_f X(s, f) P(o, f) + bias(o)                      (LIFT)
+ *   u(s, o) = sum_m G(s, m) Y(o, m) + sum_c v(s, c) Wl(o, c) + bias(o)
+ *             with Y(o, m) = Y[p][o][m mod Mo], p = m / Mo    (MID, LAST)
+ *   then u = GELU(u) when act is MBG_ACT_GELU, and
+ *   LIFT, MID: v_out = BF16(u); vhT(m, c) = BF16(sum_s F(m, s) v_out(s, c))
+ *   LAST: h(s, j) = sum_c BF16(u(s, c)) Q1(j, c) + bq1(j),
+ *         y(s) = sum_j BF16(GELU(h(s, j))) q2(j) + bq2
+ * Sizes: S a positive multiple of 128; W in 8..64 and Mo in 8..32, both
+ * multiples of 8; Fi in 1..16 (LIFT); Hq in 1..128 (LAST). */
+typedef struct mbg_fno_layer_desc {
+    int32_t mode;     /* MBG_LAYER_* */
+    int32_t act;      /* MBG_ACT_NONE or MBG_ACT_GELU */
+    int32_t batch, S, W, Mo, Fi, Hq;
+    const float* X;
+    const float* P;
+    const void* v;
+    const void* Y;
+    const void* G;
+    const void* Wl;
+    const float* bias;
+    void* v_out;
+    const void* F;
+    void* vhT;
+    const void* Q1;
+    const float* bq1;
+    const float* q2;
+    const float* bq2;
+    float* y;
+} mbg_fno_layer_desc;
+
+int mbg_fno_spectral_layer(const mbg_fno_layer_desc* d, void* stream);
 
 /* Spectral weights of one layer, wr/wi [modes][width c][width o] (FP32),
  * as the real block matrices blk[modes][2 width][2 width] (BF16) with

@@ -91,6 +91,7 @@ def load():
     # include/mbsolve_fno.h
     vp, i32, i64, f32, f64 = C.c_void_p, C.c_int32, C.c_int64, C.c_float, C.c_double
     L.mbg_fno_gemm.argtypes = [P(T.mbg_gemm_desc), vp]
+    L.mbg_fno_spectral_layer.argtypes = [P(T.mbg_fno_layer_desc), vp]
     L.mbg_fno_mode_blocks.argtypes = [vp, vp, i32, i32, vp, vp]
     L.mbg_fno_cast_bf16.argtypes = [vp, vp, i64, vp]
     L.mbg_fno_colsum.argtypes = [vp, i64, i32, i64, vp, vp]

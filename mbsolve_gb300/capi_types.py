@@ -192,3 +192,20 @@ class mbg_gemm_desc(C.Structure):
         ("c2_sm", C.c_int64), ("c2_sn", C.c_int64), ("c2_sz", C.c_int64),
         ("rowdot", C.c_void_p), ("rowdot_bias", C.c_void_p),
     ]
+
+
+MBG_LAYER_LIFT, MBG_LAYER_MID, MBG_LAYER_LAST = 0, 1, 2
+
+
+class mbg_fno_layer_desc(C.Structure):
+    _fields_ = [
+        ("mode", C.c_int32), ("act", C.c_int32),
+        ("batch", C.c_int32), ("S", C.c_int32), ("W", C.c_int32),
+        ("Mo", C.c_int32), ("Fi", C.c_int32), ("Hq", C.c_int32),
+        ("X", C.c_void_p), ("P", C.c_void_p),
+        ("v", C.c_void_p), ("Y", C.c_void_p), ("G", C.c_void_p),
+        ("Wl", C.c_void_p), ("bias", C.c_void_p),
+        ("v_out", C.c_void_p), ("F", C.c_void_p), ("vhT", C.c_void_p),
+        ("Q1", C.c_void_p), ("bq1", C.c_void_p), ("q2", C.c_void_p),
+        ("bq2", C.c_void_p), ("y", C.c_void_p),
+    ]

@@ -28,12 +28,7 @@
 #include <stdexcept>
 #include <string>
 
-#include "../../include/mbsolve_fno.h"
-#include "../../include/mbsolve_gb300.h"
-
-namespace mbg {
-void set_last_error(const char* msg);
-}
+#include "fno_common.cuh"
 
 namespace mbg {
 namespace fno {
@@ -57,10 +52,6 @@ static_assert(BM * (BN + 1) * 4 <= STAGES_GATHER * STAGE_BYTES, "epilogue tile m
 constexpr int TMEM_COLS = 64;    // power of two >= 32
 constexpr uint32_t LBO = 128;    // K-direction core-matrix stride (bytes)
 constexpr uint32_t SBO = 1024;   // M/N-direction 8-row-group stride (bytes)
-constexpr uint32_t WAIT_LIMIT = 1u << 22;
-
-constexpr uint32_t ST_WAIT = 1u;
-
 struct seg_t {
     const void* a;
     const void* b;
@@ -93,114 +84,16 @@ struct gemm_params {
     uint32_t* status;
 };
 
-// ------------------------------------------------------------ PTX wrappers
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p)
-{
-    return (uint32_t) __cvta_generic_to_shared(p);
-}
-
-// shared-memory matrix descriptor, no swizzle (layout type 0), version 1
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr)
-{
-    uint64_t d = 0;
-    d |= (uint64_t) ((addr >> 4) & 0x3FFFu);
-    d |= (uint64_t) ((LBO >> 4) & 0x3FFFu) << 16;
-    d |= (uint64_t) ((SBO >> 4) & 0x3FFFu) << 32;
-    d |= (uint64_t) 1u << 46;
-    return d;
-}
-
-// instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1),
-// A and B BF16 (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22,
-// M >> 4 at bits 24-28
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) |
-    ((uint32_t) (BN >> 3) << 17) | ((uint32_t) (BM >> 4) << 24);
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t acc)
-{
-    asm volatile(
-        "{\n"
-        ".reg .pred p;\n"
-        "setp.ne.b32 p, %4, 0;\n"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
-        "}\n" ::"r"(tmem),
-        "l"(ad), "l"(bd), "r"(IDESC), "r"(acc));
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t mbar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
-                 : "memory");
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
-}
-
-// bounded wait for the completion of the phase with the given parity
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
-{
-    for (uint32_t i = 0; i < WAIT_LIMIT; i++) {
-        uint32_t ok;
-        asm volatile(
-            "{\n"
-            ".reg .pred P;\n"
-            "mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n"
-            "selp.b32 %0, 1, 0, P;\n"
-            "}\n"
-            : "=r"(ok)
-            : "r"(mbar), "r"(parity)
-            : "memory");
-        if (ok) return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
-{
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-          "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
-}
-
 // ------------------------------------------------------------ helpers
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) { return smem_desc_nsw(addr, LBO, SBO); }
+
+constexpr uint32_t IDESC = idesc_bf16(BM, BN);
 
 __device__ __forceinline__ float ld_elem(const void* base, int32_t type, int64_t off)
 {
     if (type == MBG_BF16) return __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(base)[off]);
     return reinterpret_cast<const float*>(base)[off];
-}
-
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
-{
-    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-    return *reinterpret_cast<const uint32_t*>(&v);
-}
-
-__device__ __forceinline__ float gelu(float x)
-{
-    return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f));
-}
-
-__device__ __forceinline__ float gelu_grad(float x)
-{
-    const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
-    const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
-    return cdf + x * pdf;
 }
 
 // Gather 8 consecutive K elements (k0 .. k0+7, global K index) of row `row`
@@ -251,15 +144,6 @@ __device__ __forceinline__ void gather_chunk(
         }
     }
 }
-
-// 16 bytes global -> shared, asynchronous, L2 only; src_bytes 0 fills zeros
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes)
-{
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template<int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 // the 16-byte chunk (k0 .. k0+7) of row `row` of operand A (is_a) or B, copied
 // asynchronously to dst (zeros outside the operand); async_ok products only
@@ -450,7 +334,7 @@ __global__ void __launch_bounds__(NTH) gemm_kernel(const gemm_params p)
             for (int kk = 0; kk < BK / 16; kk++) {
                 const uint64_t ad = smem_desc(sa + (uint32_t) (kk * 256));
                 const uint64_t bd = smem_desc(sb + (uint32_t) (kk * 256));
-                mma_bf16(tmem, ad, bd, (it > 0 || kk > 0) ? 1u : 0u);
+                mma_bf16(tmem, ad, bd, IDESC, (it > 0 || kk > 0) ? 1u : 0u);
             }
             mma_commit(mb0 + 8u * st);
         }
@@ -756,27 +640,12 @@ void check_launch(const char* what)
     if (e != cudaSuccess) throw std::runtime_error(std::string("CUDA: ") + what + ": " + cudaGetErrorString(e));
 }
 
-int blocks_for(int64_t n, int per = 256)
+int blocks_for(int64_t n, int per)
 {
     int64_t b = (n + per - 1) / per;
     if (b < 1) b = 1;
     if (b > 152 * 32) b = 152 * 32;
     return (int) b;
-}
-
-template<typename F>
-int guard(F&& f)
-{
-    try {
-        f();
-        return MBG_OK;
-    } catch (const std::invalid_argument& e) {
-        set_last_error(e.what());
-        return MBG_ERR_INVALID_ARGUMENT;
-    } catch (const std::exception& e) {
-        set_last_error(e.what());
-        return MBG_ERR_CUDA;
-    }
 }
 
 void require(bool c, const char* msg)

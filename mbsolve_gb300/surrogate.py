@@ -239,10 +239,85 @@ class FNO:
         self._ibufs[B] = b
         return b
 
+    def fused_ok(self):
+        """Whether infer() can run each Fourier layer as one fused launch
+        (mbg_fno_spectral_layer): S a multiple of 128, W <= 64, 2 Mo <= 64,
+        Hq <= 128 and F <= 16."""
+        sh = self.sh
+        return (sh.S % 128 == 0 and sh.W <= 64 and 2 * sh.Mo <= 64
+                and sh.Hq <= 128 and sh.F <= 16)
+
+    def _fbuffers(self, B):
+        key = ("fused", B)
+        if key in self._ibufs:
+            return self._ibufs[key]
+        sh, d = self.sh, self.dev
+        S, W, Mo = sh.S, sh.W, sh.Mo
+        b16 = torch.bfloat16
+        b = dict(
+            v=[torch.empty(B * S * W, dtype=b16, device=d) for _ in range(2)],
+            VhT=torch.empty(B * 2 * Mo * W, dtype=b16, device=d),
+            Y=torch.empty(B * 2 * W * Mo, dtype=b16, device=d),
+            y=torch.empty(B * S, dtype=torch.float32, device=d))
+        self._ibufs[key] = b
+        return b
+
     def infer(self, X):
         """The forward pass for inference (prescreening sweeps): the same
         network and the same BF16 rounding of every product operand as
-        forward(), with the operands laid out so that every heavy product
+        forward(). Where the sizes allow (fused_ok), each Fourier layer is
+        one launch that keeps its products on chip: the lifting with the
+        first truncated DFT; the inverse DFT, pointwise mix, bias and GELU
+        with the next DFT; the last layer with the projection and the
+        output layer. Between them one product per layer mixes the modes
+        of all samples (M = batch, N = 2 W, per mode), writing the mixed
+        spectrum as BF16 [B, 2, W, Mo]. Otherwise the products of
+        _infer_products run. X: FP32 [B, S, F]; returns y [B, S] (a view of
+        an internal buffer)."""
+        sh = self.sh
+        S, W, Mo, L, Fi, Hq = sh.S, sh.W, sh.Mo, sh.L, sh.F, sh.Hq
+        B = X.shape[0]
+        if tuple(X.shape) != (B, S, Fi) or X.dtype != torch.float32:
+            raise ValueError("X must be FP32 [B, %d, %d]" % (S, Fi))
+        if not self.fused_ok():
+            return self._infer_products(X)
+        X = X.contiguous()
+        b = self._fbuffers(B)
+        p = self.p
+        if not self._blk_valid:
+            self._mode_blocks()
+        wb = self._wb
+        vhT, Y = b["VhT"], b["Y"]
+        K.spectral_layer(T.MBG_LAYER_LIFT, T.MBG_ACT_NONE, B, S, W, Mo, Fi=Fi,
+                         X=X, P=p["P"], bias=p["bp"], v_out=b["v"][0],
+                         F=self.F, vhT=vhT)
+        cur = 0
+        for l in range(L):
+            # mode mixing, per mode m: Y[b, :, :, m] = blk[m] [Re; Im]
+            blk = self.blk[l]
+            K.gemm(B, 2 * W,
+                   [Seg(vhT, 0, 2 * Mo * W, 1, W, blk, 0, 2 * W, 1, 4 * W * W, W),
+                    Seg(vhT, Mo * W, 2 * Mo * W, 1, W, blk, W, 2 * W, 1, 4 * W * W, W)],
+                   Y, 0, 2 * W * Mo, Mo, 1, batch=Mo)
+            if l < L - 1:
+                K.spectral_layer(T.MBG_LAYER_MID, T.MBG_ACT_GELU, B, S, W, Mo,
+                                 v=b["v"][cur], Y=Y, G=self.G, Wl=wb["W%d" % l],
+                                 bias=p["bw%d" % l], v_out=b["v"][1 - cur],
+                                 F=self.F, vhT=vhT)
+                cur = 1 - cur
+            else:
+                K.spectral_layer(T.MBG_LAYER_LAST, T.MBG_ACT_NONE, B, S, W, Mo,
+                                 Hq=Hq, v=b["v"][cur], Y=Y, G=self.G,
+                                 Wl=wb["W%d" % l], bias=p["bw%d" % l],
+                                 Q1=wb["Q1"], bq1=p["bq1"], q2=p["q2"],
+                                 bq2=p["bq2"], y=b["y"])
+        return b["y"].view(B, S)
+
+    def _infer_products(self, X):
+        """infer() for sizes the fused layer kernel does not take, as
+        products of the general kernel: the same network and the same BF16
+        rounding of every product operand as forward(), with the operands
+        laid out so that every heavy product
         reads BF16 with K contiguous (the GEMM then stages them by
         asynchronous copies, four stages deep): each activation is kept as
         [B, S, W] and, written by the same epilogue, as [B, W, S]; the mixed
@@ -255,8 +330,6 @@ class FNO:
         sh = self.sh
         S, W, Mo, L, Fi, Hq = sh.S, sh.W, sh.Mo, sh.L, sh.F, sh.Hq
         B = X.shape[0]
-        if tuple(X.shape) != (B, S, Fi) or X.dtype != torch.float32:
-            raise ValueError("X must be FP32 [B, %d, %d]" % (S, Fi))
         X = X.contiguous()
         b = self._ibuffers(B)
         p = self.p

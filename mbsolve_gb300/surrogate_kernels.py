@@ -117,6 +117,50 @@ def gemm(m, n, segs, c, c_off, c_sm, c_sn, c_sz=0, batch=1,
     _native.check(_lib().mbg_fno_gemm(C.byref(d), _stream()))
 
 
+def spectral_layer(mode, act, batch, S, W, Mo, Fi=0, Hq=0, X=None, P=None,
+                   v=None, Y=None, G=None, Wl=None, bias=None, v_out=None,
+                   F=None, vhT=None, Q1=None, bq1=None, q2=None, bq2=None,
+                   y=None):
+    """One Fourier layer of inference in one launch (mbg_fno_spectral_layer):
+    mode MBG_LAYER_LIFT (X [B, S, Fi], P [W, Fi] FP32), MBG_LAYER_MID (v
+    [B, S, W], Y [B, 2, W, Mo], G [S, 2 Mo], Wl [W, W] BF16) or
+    MBG_LAYER_LAST (the same plus Q1 [Hq, W] BF16, bq1, q2 [Hq], bq2 [1]
+    FP32, y [B, S] FP32); LIFT and MID write v_out [B, S, W] and the
+    spectrum vhT [B, 2 Mo, W] (BF16) with F [2 Mo, S] BF16."""
+    B = int(batch)
+    need = {}
+    if mode == T.MBG_LAYER_LIFT:
+        need.update(X=(X, torch.float32, B * S * Fi), P=(P, torch.float32, W * Fi))
+    else:
+        need.update(v=(v, torch.bfloat16, B * S * W),
+                    Y=(Y, torch.bfloat16, B * 2 * W * Mo),
+                    G=(G, torch.bfloat16, S * 2 * Mo),
+                    Wl=(Wl, torch.bfloat16, W * W))
+    if mode == T.MBG_LAYER_LAST:
+        need.update(Q1=(Q1, torch.bfloat16, Hq * W), bq1=(bq1, torch.float32, Hq),
+                    q2=(q2, torch.float32, Hq), bq2=(bq2, torch.float32, 1),
+                    y=(y, torch.float32, B * S))
+    else:
+        need.update(v_out=(v_out, torch.bfloat16, B * S * W),
+                    F=(F, torch.bfloat16, 2 * Mo * S),
+                    vhT=(vhT, torch.bfloat16, B * 2 * Mo * W))
+    if bias is not None:
+        need["bias"] = (bias, torch.float32, W)
+    d = T.mbg_fno_layer_desc()
+    for name, (t, dt, n) in need.items():
+        if t is None:
+            raise ValueError("spectral_layer: %s is required" % name)
+        if t.dtype != dt or not t.is_cuda or not t.is_contiguous():
+            raise ValueError("spectral_layer %s: contiguous CUDA %s" % (name, dt))
+        if t.numel() < n:
+            raise ValueError("spectral_layer %s: %d elements, %d needed"
+                             % (name, t.numel(), n))
+        setattr(d, name, _ptr(t))
+    d.mode, d.act, d.batch = int(mode), int(act), B
+    d.S, d.W, d.Mo, d.Fi, d.Hq = int(S), int(W), int(Mo), int(Fi), int(Hq)
+    _native.check(_lib().mbg_fno_spectral_layer(C.byref(d), _stream()))
+
+
 def mode_blocks(wr, wi, blk):
     modes, width = wr.shape[0], wr.shape[1]
     if blk.dtype != torch.bfloat16 or blk.numel() < modes * 4 * width * width:

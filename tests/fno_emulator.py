@@ -58,6 +58,45 @@ def gemm(m, n, segs, c, c_off, c_sm, c_sn, c_sz=0, batch=1, mode=0, act=0,
         _view(c2, 0, (batch, m, n), (c2_sz, c2_sm, c2_sn)).copy_(v.to(c2.dtype))
 
 
+def _gelu(v):
+    return 0.5 * v * (1.0 + torch.erf(v / math.sqrt(2.0)))
+
+
+def _flat(t, n, shape):
+    return t.reshape(-1)[:n].reshape(shape)
+
+
+def spectral_layer(mode, act, batch, S, W, Mo, Fi=0, Hq=0, X=None, P=None,
+                   v=None, Y=None, G=None, Wl=None, bias=None, v_out=None,
+                   F=None, vhT=None, Q1=None, bq1=None, q2=None, bq2=None,
+                   y=None):
+    B, M2 = batch, 2 * Mo
+    f32, f64, b16 = torch.float32, torch.float64, torch.bfloat16
+    if mode == 0:
+        u = _bf(_flat(X, B * S * Fi, (B, S, Fi))) @ _bf(_flat(P, W * Fi, (W, Fi))).T
+    else:
+        Yv = _bf(_flat(Y, B * 2 * W * Mo, (B, 2, W, Mo)))
+        Yf = torch.cat([Yv[:, 0], Yv[:, 1]], dim=2)            # [B, W, 2 Mo]
+        u = _bf(_flat(G, S * M2, (S, M2))) @ Yf.transpose(1, 2) + \
+            _bf(_flat(v, B * S * W, (B, S, W))) @ _bf(_flat(Wl, W * W, (W, W))).T
+    u = u.to(f32).to(f64)                                      # FP32 accumulator
+    if bias is not None:
+        u = (u + bias[:W].to(f64)).to(f32).to(f64)
+    if act == 1:
+        u = _gelu(u)
+    ub = _bf(u)
+    if mode != 2:
+        v_out.reshape(-1)[:B * S * W].copy_(ub.reshape(-1).to(b16))
+        d = (_bf(_flat(F, M2 * S, (M2, S))) @ ub).to(f32)      # [B, 2 Mo, W]
+        vhT.reshape(-1)[:B * M2 * W].copy_(d.reshape(-1).to(b16))
+    else:
+        h = (ub @ _bf(_flat(Q1, Hq * W, (Hq, W))).T).to(f32).to(f64)
+        h = (h + bq1[:Hq].to(f64)).to(f32).to(f64)
+        z = _bf(_gelu(h))
+        yv = (z * _bf(q2[:Hq].to(f64))).sum(-1) + bq2[0].to(f64)
+        y.reshape(-1)[:B * S].copy_(yv.reshape(-1).to(f32))
+
+
 def cast_bf16(x, y):
     y.copy_(x.reshape(-1)[:y.numel()].to(torch.bfloat16))
 
@@ -94,5 +133,6 @@ def adam(w, g, m, v, lr, beta1, beta2, eps, weight_decay, step):
 def install(monkeypatch):
     """Route the surrogate module's kernel calls to this model."""
     from mbsolve_gb300 import surrogate as S
-    for name in ("gemm", "mode_blocks", "colsum", "mse", "adam", "cast_bf16"):
+    for name in ("gemm", "spectral_layer", "mode_blocks", "colsum", "mse",
+                 "adam", "cast_bf16"):
         monkeypatch.setattr(S.K, name, globals()[name])

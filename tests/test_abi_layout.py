@@ -14,7 +14,7 @@ from mbsolve_gb300 import capi_types as T
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 STRUCTS = ["mbg_qm", "mbg_material", "mbg_region", "mbg_device", "mbg_source",
            "mbg_record", "mbg_scenario", "mbg_grid", "mbg_tuning",
-           "mbg_gemm_segment", "mbg_gemm_desc"]
+           "mbg_gemm_segment", "mbg_gemm_desc", "mbg_fno_layer_desc"]
 
 
 @pytest.mark.skipif(shutil.which("gcc") is None, reason="no C compiler")

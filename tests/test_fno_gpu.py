@@ -135,14 +135,19 @@ def test_training_fits_a_pulse_operator(S):
     assert last < first / 20, (first, last)
 
 
-@pytest.mark.parametrize("args,B", [(dict(S=128, W=16, Mo=8, L=2, F=8, Hq=32), 16),
-                                    ({}, 24)])
-def test_inference_path_matches_forward_and_oracle(S, args, B):
-    """FNO.infer (BF16 operands with K contiguous, staged by asynchronous
-    copies; the DFT as one product without split-K) equals forward() and
-    the oracle's bf16-mode output; two calls in a row give the same."""
+@pytest.mark.parametrize("args,B,fused", [
+    (dict(S=128, W=16, Mo=8, L=2, F=8, Hq=32), 16, True),
+    (dict(S=128, W=72, Mo=8, L=2, F=8, Hq=32), 8, False),
+    ({}, 24, True), ({}, 200, True)])
+def test_inference_path_matches_forward_and_oracle(S, args, B, fused):
+    """FNO.infer (fused layer launches where the sizes allow, else products
+    of the general kernel with BF16 operands, K contiguous) equals
+    forward() and the oracle's bf16-mode output; two calls in a row give
+    the same. Batch 200 puts two samples on some CTAs of the fused
+    kernel."""
     sh = S.Shapes(**args)
     net = S.FNO(sh, seed=5)
+    assert net.fused_ok() == fused
     rng = np.random.default_rng(12)
     X = torch.tensor(rng.normal(size=(B, sh.S, sh.F)).astype(np.float32),
                      device="cuda")

@@ -84,18 +84,47 @@ def test_sweep_space_is_deterministic():
     assert sce.get_num_gridpoints() == a.n_x
 
 
-def test_inference_plan_equals_forward(monkeypatch):
-    """FNO.infer's products (K-contiguous BF16 layouts, the transposed
-    activation copies, the mixed spectrum as [B, W, 2 Mo], BF16 weight
-    copies) compute the same network as forward(), through the CPU model
-    of the kernels."""
+@pytest.mark.parametrize("S_,fused", [(64, False), (128, True)])
+def test_inference_plan_equals_forward(monkeypatch, S_, fused):
+    """FNO.infer computes the same network as forward(), through the CPU
+    model of the kernels: as fused layer launches (S a multiple of 128:
+    lifting + DFT, inverse DFT + pointwise + DFT, last layer + projection,
+    one mixing product per layer) and as products of the general kernel
+    (K-contiguous BF16 layouts, transposed activation copies, BF16 weight
+    copies)."""
     from mbsolve_gb300 import surrogate as S
     E.install(monkeypatch)
-    sh = S.Shapes(S=64, W=16, Mo=8, L=3, F=5, Hq=24)
+    sh = S.Shapes(S=S_, W=16, Mo=8, L=3, F=5, Hq=24)
     net = S.FNO(sh, seed=2, device="cpu")
-    X = torch.tensor(np.random.default_rng(4).normal(size=(3, 64, 5)),
+    assert net.fused_ok() == fused
+    X = torch.tensor(np.random.default_rng(4).normal(size=(3, S_, 5)),
                      dtype=torch.float32)
     yf = net.forward(X).clone().double().numpy()
     yi = net.infer(X).clone().double().numpy()
     assert np.linalg.norm(yi - yf) <= 1e-6 * np.linalg.norm(yf)
 
+
+
+def test_spectral_layer_refuses_bad_sizes():
+    """The fused layer's C entry point checks sizes and operands before it
+    touches the GPU."""
+    import ctypes as C
+    from mbsolve_gb300 import _native
+    from mbsolve_gb300 import capi_types as T
+    L = _native.load()
+    good = dict(mode=T.MBG_LAYER_MID, act=T.MBG_ACT_GELU, batch=4, S=256,
+                W=64, Mo=32, Fi=0, Hq=0)
+    bad = [dict(S=200), dict(W=72), dict(W=12), dict(Mo=40), dict(Mo=12),
+           dict(mode=7), dict(act=2), dict(batch=0)]
+    for b in bad:
+        d = T.mbg_fno_layer_desc()
+        for k, v in dict(good, **b).items():
+            setattr(d, k, v)
+        rc = L.mbg_fno_spectral_layer(C.byref(d), None)
+        assert rc == T.MBG_ERR_INVALID_ARGUMENT, b
+    d = T.mbg_fno_layer_desc()       # sizes fine, operands missing
+    for k, v in good.items():
+        setattr(d, k, v)
+    assert L.mbg_fno_spectral_layer(C.byref(d), None) == T.MBG_ERR_INVALID_ARGUMENT
+    assert b"v, Y, G and Wl" in L.mbg_last_error()
+    assert L.mbg_fno_spectral_layer(None, None) == T.MBG_ERR_INVALID_ARGUMENT
