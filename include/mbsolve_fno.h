@@ -112,17 +112,26 @@ enum {
 
 /* One Fourier layer of inference for every sample in one launch, the
  * layer's products kept on chip (one CTA per SM owns whole samples).
- * Layouts, row-major, BF16 unless stated, all 16-byte aligned:
- *   X [B][S][Fi] FP32, P [W][Fi] FP32        (LIFT)
- *   v [B][S][W], Y [B][2][W][Mo] (Re then Im of the mixed spectrum),
- *   G [S][2 Mo], Wl [W][W]                   (MID, LAST)
- *   bias [W] FP32 (NULL: zero)
- *   F [2 Mo][S], v_out [B][S][W], vhT [B][2 Mo][W]   (LIFT, MID)
- *   Q1 [Hq][W], bq1 [Hq], q2 [Hq], bq2 [1] FP32, y [B][S] FP32   (LAST)
+ * Tile images: a matrix stored as its K-major core-matrix image, element
+ * (r, k) of an R x K block at ((r/8) (K/8) + k/8) 64 + (r%8) 8 + k%8
+ * (mbg_fno_image_bf16 writes them). T = S / 128 tiles per sample.
+ *   v, v_out  activations: for sample b and tile i the 128 x 64 image of
+ *             rows 128 i .. 128 i + 127 (channels W..63 zero) at
+ *             (b T + i) 8192 (BF16, B S 64 elements)
+ *   G         inverse DFT basis [S][2 Mo]: the 128 x 64 image of tile i's
+ *             rows at i 8192 (columns 2 Mo..63 zero)
+ *   F         forward DFT basis [2 Mo][S]: the 64 x 128 image of tile i's
+ *             columns at i 8192 (rows 2 Mo..63 zero)
+ *   Wl        pointwise weights [W][W]: their 64 x 64 image
+ *   Q1        projection weights [Hq][W]: their 128 x 64 image
+ * Plain layouts (row-major): X [B][S][Fi] FP32, P [W][Fi] FP32,
+ * Y [B][2][Mo][W] BF16 (Re then Im of the mixed spectrum), bias [W] FP32
+ * (NULL: zero), vhT [B][2 Mo][W] BF16, bq1, q2 [Hq], bq2 [1], y [B][S]
+ * FP32. Every pointer 16-byte aligned.
  * Arithmetic: every product operand rounded to BF16, FP32 accumulation.
  *   u(s, o) = sum_f X(s, f) P(o, f) + bias(o)                      (LIFT)
  *   u(s, o) = sum_m G(s, m) Y(o, m) + sum_c v(s, c) Wl(o, c) + bias(o)
- *             with Y(o, m) = Y[p][o][m mod Mo], p = m / Mo    (MID, LAST)
+ *             with Y(o, m) = Y[p][m mod Mo][o], p = m / Mo    (MID, LAST)
  *   then u = GELU(u) when act is MBG_ACT_GELU, and
  *   LIFT, MID: v_out = BF16(u); vhT(m, c) = BF16(sum_s F(m, s) v_out(s, c))
  *   LAST: h(s, j) = sum_c BF16(u(s, c)) Q1(j, c) + bq1(j),
@@ -159,6 +168,15 @@ int mbg_fno_mode_blocks(const float* wr, const float* wi, int32_t modes,
                         int32_t width, void* blk, void* stream);
 
 int mbg_fno_cast_bf16(const float* x, void* y, int64_t n, void* stream);
+
+/* K-major core-matrix image (the operand layout of
+ * mbg_fno_spectral_layer): for z < batch, the R x K matrix whose (r, c)
+ * entry is x[z zs + r ld + c] for r < rows, c < cols and zero elsewhere,
+ * as BF16 at img + z R K with (r, c) at ((r/8) (K/8) + c/8) 64 +
+ * (r%8) 8 + c%8. R, K multiples of 8. */
+int mbg_fno_image_bf16(const float* x, int32_t batch, int32_t rows,
+                       int32_t cols, int64_t ld, int64_t zs, int32_t R,
+                       int32_t K, void* img, void* stream);
 
 /* out[j] += sum_i x[i row_stride + j], i < rows, j < cols (FP32) */
 int mbg_fno_colsum(const float* x, int64_t rows, int32_t cols,

@@ -94,6 +94,8 @@ def load():
     L.mbg_fno_spectral_layer.argtypes = [P(T.mbg_fno_layer_desc), vp]
     L.mbg_fno_mode_blocks.argtypes = [vp, vp, i32, i32, vp, vp]
     L.mbg_fno_cast_bf16.argtypes = [vp, vp, i64, vp]
+    L.mbg_fno_image_bf16.argtypes = [vp, i32, i32, i32, i64, i64, i32, i32,
+                                     vp, vp]
     L.mbg_fno_colsum.argtypes = [vp, i64, i32, i64, vp, vp]
     L.mbg_fno_mse.argtypes = [vp, vp, i64, vp, vp, vp]
     L.mbg_fno_adam.argtypes = [vp, vp, vp, vp, i64, f32, f32, f32, f32, f32,

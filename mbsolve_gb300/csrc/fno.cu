@@ -538,6 +538,21 @@ __global__ void cast_kernel(const float* x, __nv_bfloat16* y, int64_t n)
         y[i] = __float2bfloat16_rn(x[i]);
 }
 
+// img[z] = the K-major core-matrix image of the R x K matrix whose (r, c)
+// entry is x[z zs + r ld + c] (zero outside rows x cols), as BF16
+__global__ void image_kernel(const float* x, int batch, int rows, int cols, int64_t ld, int64_t zs, int R, int K,
+                             __nv_bfloat16* img)
+{
+    const int64_t per = (int64_t) R * K, total = per * batch;
+    for (int64_t t = blockIdx.x * (int64_t) blockDim.x + threadIdx.x; t < total;
+         t += (int64_t) gridDim.x * blockDim.x) {
+        const int64_t z = t / per, e = t % per;
+        const int blk = (int) (e >> 6), r = (blk / (K / 8)) * 8 + (int) ((e >> 3) & 7),
+                  c = (blk % (K / 8)) * 8 + (int) (e & 7);
+        img[t] = __float2bfloat16_rn(r < rows && c < cols ? x[z * zs + r * ld + c] : 0.0f);
+    }
+}
+
 // one CTA per (column, row slice): strided partial sums, then atomics
 __global__ void colsum_kernel(const float* x, int64_t rows, int cols, int64_t rs, float* out)
 {
@@ -788,6 +803,20 @@ int mbg_fno_cast_bf16(const float* x, void* y, int64_t n, void* stream)
         require(x && y && n > 0, "cast_bf16: bad arguments");
         cast_kernel<<<blocks_for(n), 256, 0, (cudaStream_t) stream>>>(x, (__nv_bfloat16*) y, n);
         check_launch("cast_kernel");
+    });
+}
+
+int mbg_fno_image_bf16(const float* x, int32_t batch, int32_t rows, int32_t cols, int64_t ld, int64_t zs,
+                       int32_t R, int32_t K, void* img, void* stream)
+{
+    return guard([&] {
+        require(x && img && batch > 0 && rows > 0 && cols > 0, "image_bf16: bad arguments");
+        require(R >= rows && K >= cols && R % 8 == 0 && K % 8 == 0, "image_bf16: R, K must cover rows, cols and be multiples of 8");
+        require(ld >= cols && (batch == 1 || zs > 0), "image_bf16: bad strides");
+        const int64_t n = (int64_t) batch * R * K;
+        image_kernel<<<blocks_for(n), 256, 0, (cudaStream_t) stream>>>(x, batch, rows, cols, ld, zs, R, K,
+                                                                       (__nv_bfloat16*) img);
+        check_launch("image_kernel");
     });
 }
 

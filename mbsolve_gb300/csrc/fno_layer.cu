@@ -18,25 +18,28 @@
 //                   H = v_tile Q1^T, whose epilogue reduces GELU(H + bq1)
 //                   against q2 into the output y
 //
-// Pipeline: one iteration per tile t, 8 warps in lock step, one thread
-// issuing the MMAs. In iteration t the first product of tile t is issued,
-// the epilogue of tile t-1 runs, the second product of tile t-1 is issued
-// and the second product of tile t-3 is read out; the per-sample
-// activations of tile t+2 (v, or X) and the shared operands of tile t+1
-// (the G and DFT-basis tiles, L2-resident) are copied (cp.async) meanwhile.
-// So no step waits for work issued less than an iteration before it: the
-// rings hold three v (four X) tiles, two G tiles, four basis tiles and
-// three Y tiles; TMEM holds two first-product accumulators and two
-// second-product ones; the MMA operands written by the epilogue are
-// double-buffered. Operand tiles use the no-swizzle K-major core-matrix
-// layout. The transposed activation tile (K = samples) has its K-direction
-// core matrices 144 bytes apart instead of 128, so that a warp's 2-byte
-// stores of one channel for 32 consecutive samples land in four distinct
-// bank groups. The DFT product has M = 64 mode rows; it is issued as
-// M = 128, and the 64 rows above the basis tile read whatever lies behind
-// it in shared memory: they only feed TMEM lanes 64-127, which nothing
-// reads. Every wait is bounded; on time-out the kernel records it in the
-// status word and returns after freeing its TMEM.
+// Warp roles, coupled only by mbarriers (no block-wide barrier inside the
+// tile loop): warp 16 stages operands by bulk copies (TMA engine, one
+// instruction per 16 KB tile image) into rings of two (G, v) pairs (six X
+// tiles for the lifting) and four DFT-basis tiles, and transposes a
+// sample's mixed spectrum Y into its operand image; one thread of warp 17
+// issues the MMAs into two first-product and two
+// second-product TMEM accumulators; warps 0-15 run the epilogues (warp w
+// reads TMEM lanes 32 (w % 4) .. +31, columns 16 (w / 4) .. +15) and write
+// each output tile as an image in shared memory that one bulk copy stores.
+// Activations, the DFT bases and the dense weights are kept as K-major
+// core-matrix images (8 rows x 16 bytes per core matrix, no swizzle), the
+// layout the MMA reads, so a tile moves between HBM and shared memory as
+// one contiguous block. The transposed activation tile (K = samples) is
+// written by 2-byte stores; its K-direction core matrices are 144 bytes
+// apart instead of 128, so that a warp's stores of one channel for 32
+// consecutive samples land in four distinct bank groups. The DFT product
+// has M = 64 mode rows; it is issued as M = 128, and the 64 rows above the
+// basis tile read whatever lies behind it in shared memory: they only feed
+// TMEM lanes 64-127, which nothing reads. Every wait is bounded; when one
+// runs out the kernel raises an abort flag that ends every other wait,
+// records the failure in the status word and returns after freeing its
+// TMEM.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -49,44 +52,58 @@ namespace mbg {
 namespace fno {
 namespace {
 
-constexpr int LT = 128;    // rows (samples s) per tile
-constexpr int LNTH = 256;  // warp w: TMEM lanes 32 (w % 4) .. +31, columns 32 (w / 4) .. +31
+constexpr int LT = 128;                   // rows (samples s) per tile
+constexpr int NEPI = 512;                 // epilogue threads: warps 0-15
+constexpr int PROD_WARP = 16, MMA_WARP = 17;
+constexpr int LNTH = 576;
 
-constexpr int F_TILE = 64 * LT * 2;             // DFT basis tile: 64 mode rows x 128 samples
-constexpr int X_TILE = LT * 16 * 4;             // lifting input tile: 128 rows x <= 16 FP32 features
-constexpr int NF = 4, NG = 2, NV = 3, NX = 4, NY = 3;  // ring depths
-constexpr uint32_t VT_LBO = 144;                // transposed tile: K-direction core-matrix stride
-constexpr uint32_t VT_SBO = 16 * VT_LBO;        // 8-channel group stride
-constexpr int VT_TILE = 8 * VT_SBO;             // 64 channel rows x 128 samples
-constexpr int A_TILE = LT * 64 * 2;             // G, v or projection-input tile: 128 rows x K 64
-constexpr int B_TILE = 64 * 64 * 2;             // Y or Wl tile: 64 rows x K 64
-constexpr int Q_TILE = 128 * 64 * 2;            // Q1 tile: 128 rows x K 64
+constexpr int IMG = 128 * 64 * 2;         // 128 x 64 BF16 image: v, G, projection input, Q1
+constexpr int F_IMG = 64 * LT * 2;        // 64 mode rows x 128 samples
+constexpr int B_IMG = 64 * 64 * 2;        // Y or Wl
+constexpr int IMG_ELEMS = IMG / 2;
+constexpr int NGV = 2, NX = 6, NFR = 4, NYR = 2;  // ring depths: (G, v) pairs, X tiles (LIFT), basis tiles, Y
+constexpr int X_SLOT = LT * 16 * 4;       // lifting input tile: 128 rows x <= 16 FP32 features
+constexpr uint32_t VT_LBO = 144;          // transposed tile: K-direction core-matrix stride
+constexpr uint32_t VT_SBO = 16 * VT_LBO;  // 8-channel group stride
+constexpr int VT_IMG = 8 * VT_SBO;        // 64 channel rows x 128 samples
 
-// shared memory map (bytes from a 128-aligned base); LAST keeps Q1 where
-// the basis ring is, its projection inputs where the transposed tiles
-// are; LIFT keeps its X ring where the v ring is
-constexpr int OFF_F = 0;
-constexpr int OFF_Q = 0;
-constexpr int OFF_VT = OFF_F + NF * F_TILE;
-constexpr int OFF_G = OFF_VT + 2 * VT_TILE;
-constexpr int OFF_V = OFF_G + NG * A_TILE;
-constexpr int OFF_X = OFF_V;
-constexpr int OFF_Y = OFF_V + NV * A_TILE;
-constexpr int OFF_W = OFF_Y + NY * B_TILE;
-constexpr int OFF_SMALL = OFF_W + B_TILE;
-constexpr int SM_BIAS = 0, SM_BQ1 = 64, SM_Q2 = 192, SM_RED = 320, SM_P = 448;  // floats
+// shared memory map (bytes from a 128-aligned base); LAST keeps Q1 in the
+// basis ring and its two projection-input images where the transposed
+// tiles are
+constexpr int GV_SLOT = 2 * IMG;
+constexpr int OFF_GV = 0;
+constexpr int OFF_F = OFF_GV + NGV * GV_SLOT;
+constexpr int OFF_Q = OFF_F;
+constexpr int OFF_VT = OFF_F + NFR * F_IMG;  // two transposed tiles (LAST: projection inputs)
+constexpr int OFF_OUT = OFF_VT + 2 * VT_IMG;  // output image (LIFT, MID)
+constexpr int OFF_Y = OFF_OUT + IMG;
+constexpr int OFF_W = OFF_Y + NYR * B_IMG;
+constexpr int OFF_SMALL = OFF_W + B_IMG;
+constexpr int SM_BIAS = 0, SM_BQ1 = 64, SM_Q2 = 192, SM_RED = 320, SM_P = 1344;  // floats
 constexpr int SMALL_FLOATS = SM_P + 16 * 64;
 constexpr int LAYER_SMEM = OFF_SMALL + SMALL_FLOATS * 4 + 128;  // + alignment slack
 // the last basis slot's unread M rows (32 KB from its start) stay inside the map
-static_assert(OFF_F + (NF - 1) * F_TILE + 2 * F_TILE <= OFF_G, "basis slot overrun");
-static_assert(Q_TILE <= NF * F_TILE && 2 * A_TILE <= 2 * VT_TILE && NX * X_TILE <= NV * A_TILE, "aliases");
-static_assert(LAYER_SMEM + 128 <= 227 * 1024, "shared memory");
+static_assert(OFF_F + (NFR - 1) * F_IMG + 2 * F_IMG <= OFF_OUT, "basis slot overrun");
+static_assert(NX * X_SLOT <= NGV * GV_SLOT && IMG <= NFR * F_IMG && IMG <= VT_IMG, "aliases");
+static_assert(LAYER_SMEM + 512 <= 227 * 1024, "shared memory");
 
 constexpr uint32_t ID64 = idesc_bf16(128, 64);
 constexpr uint32_t ID128 = idesc_bf16(128, 128);
 // columns: first-product accumulators at 0 and 64; DFT accumulators at 128
 // and 192 (by sample parity); projection accumulators at 256 and 384
 constexpr uint32_t LAYER_TMEM_COLS = 512;
+
+// mbarriers: full (data ready) / empty (slot free) pairs
+enum {
+    B_FGV = 0, B_EGV = 6,    // (G, v) / X ring: bulk bytes / inverse MMA (LIFT: the epilogue warps read X)
+    B_FF = 12, B_EF = 16,    // basis ring: bulk bytes / DFT MMA
+    B_FY = 20, B_EY = 22,    // Y ring: copy warp / a sample's last inverse MMA
+    B_FACC = 24, B_EACC = 26,  // first-product accumulators: MMA / epilogue warps
+    B_FOP = 28, B_EOP = 30,  // epilogue-written MMA operand: epilogue warps / second-product MMA
+    B_FD = 32, B_ED = 34,    // DFT accumulators: a sample's last DFT MMA / epilogue warps
+    B_FH = 36, B_EH = 38,    // projection accumulators: MMA / epilogue warps
+    NBAR = 40
+};
 
 struct layer_params {
     int32_t mode, act, batch, S, W, Mo, Fi, Hq;
@@ -108,7 +125,7 @@ struct layer_params {
     uint32_t* status;
 };
 
-// byte offset of 16-byte chunk (row, kc) in a K-major tile with `kch`
+// byte offset of 16-byte chunk (row, kc) in a K-major image with `kch`
 // chunks per row (core matrices 128 bytes apart along K)
 __device__ __forceinline__ uint32_t koff(int row, int kc, int kch)
 {
@@ -128,88 +145,46 @@ __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t
                  : "memory");
 }
 
-// the sample (global index) of this CTA's tile u
-__device__ __forceinline__ int64_t tile_sample(int u, int T)
+// bounded wait; gives up at once when another wait has run out
+__device__ __forceinline__ bool wait_bar(uint32_t mbar, uint32_t parity, volatile int* abort)
 {
-    return blockIdx.x + (int64_t) (u / T) * gridDim.x;
+    for (uint32_t i = 0; i < WAIT_LIMIT; i++) {
+        if (mbar_test(mbar, parity)) return true;
+        if (*abort) return false;
+    }
+    *abort = 1;
+    return false;
 }
 
-// Shared operands of tile u: its G tile (MID, LAST) and DFT-basis tile
-// (LIFT, MID), both the same for every sample; chunks outside the operands
-// are zero-filled.
-__device__ __forceinline__ void copy_shared_ops(const layer_params& p, int u, int T, uint32_t sb, int tid)
+// the same, polled by lane 0 for the whole warp
+__device__ __forceinline__ bool wait_bar_warp(uint32_t mbar, uint32_t parity, volatile int* abort, int lane)
 {
-    const int s0 = (u % T) * LT, two_mo = 2 * p.Mo;
-    if (p.mode != MBG_LAYER_LIFT) {
-        const uint32_t sg = sb + OFF_G + (uint32_t) ((u % NG) * A_TILE);
-#pragma unroll
-        for (int q = 0; q < 1024 / LNTH; q++) {
-            const int e = tid + q * LNTH, r = e >> 3, kc = e & 7;
-            const bool ok = kc * 8 < two_mo;
-            cp_async16(sg + koff(r, kc, 8), ok ? p.G + (int64_t) (s0 + r) * two_mo + kc * 8 : p.G, ok ? 16u : 0u);
-        }
-    }
-    if (p.mode != MBG_LAYER_LAST) {
-        const uint32_t sf = sb + OFF_F + (uint32_t) ((u % NF) * F_TILE);
-#pragma unroll
-        for (int q = 0; q < 1024 / LNTH; q++) {
-            const int e = tid + q * LNTH, r = e >> 4, kc = e & 15;
-            const bool ok = r < two_mo;
-            cp_async16(sf + koff(r, kc, 16), ok ? p.F + (int64_t) r * p.S + s0 + kc * 8 : p.F, ok ? 16u : 0u);
-        }
-    }
+    int ok = 0;
+    if (lane == 0) ok = wait_bar(mbar, parity, abort) ? 1 : 0;
+    return __shfl_sync(0xFFFFFFFFu, ok, 0) != 0;
 }
 
-// Per-sample operands of tile u: its v tile and, for a sample's first
-// tile, the sample's Y (MID, LAST), or its X tile (LIFT).
-__device__ __forceinline__ void copy_sample_ops(const layer_params& p, int u, int T, uint32_t sb, int tid)
-{
-    const int i = u % T, s0 = i * LT, two_mo = 2 * p.Mo;
-    const int64_t b = tile_sample(u, T);
-    if (p.mode == MBG_LAYER_LIFT) {
-        // the tile's X rows are contiguous: 128 Fi floats, 16-byte aligned
-        const float* xs = p.X + (b * p.S + s0) * p.Fi;
-        const uint32_t sx = sb + OFF_X + (uint32_t) ((u % NX) * X_TILE);
-        for (int e = tid; e < LT * p.Fi / 4; e += LNTH) cp_async16(sx + e * 16, xs + e * 4, 16u);
-        return;
-    }
-    const uint32_t sv = sb + OFF_V + (uint32_t) ((u % NV) * A_TILE);
-#pragma unroll
-    for (int q = 0; q < 1024 / LNTH; q++) {
-        const int e = tid + q * LNTH, r = e >> 3, kc = e & 7;
-        const bool ok = kc * 8 < p.W;
-        cp_async16(sv + koff(r, kc, 8), ok ? p.v + (b * p.S + s0 + r) * p.W + kc * 8 : p.v, ok ? 16u : 0u);
-    }
-    if (i == 0) {
-        const uint32_t sy = sb + OFF_Y + (uint32_t) (((u / T) % NY) * B_TILE);
-#pragma unroll
-        for (int q = 0; q < 512 / LNTH; q++) {
-            const int e = tid + q * LNTH, o = e >> 3, kc = e & 7, k = kc * 8;
-            const bool ok = o < p.W && k < two_mo;
-            const int part = ok ? k / p.Mo : 0, m = ok ? k % p.Mo : 0;
-            cp_async16(sy + koff(o, kc, 8), ok ? p.Y + ((b * 2 + part) * p.W + o) * p.Mo + m : p.Y, ok ? 16u : 0u);
-        }
-    }
-}
-
+template<int MODE, bool GELU>
 __global__ void __launch_bounds__(LNTH, 1) spectral_layer_kernel(const layer_params p)
 {
     extern __shared__ __align__(128) uint8_t smem_raw[];
-    // first product of an even / odd tile, second product of an even / odd tile
-    __shared__ __align__(8) uint64_t mbar[4];
+    __shared__ __align__(8) uint64_t mbar[NBAR];
     __shared__ uint32_t tmem_sh;
+    __shared__ int abort_sh;
 
+    constexpr bool lift = MODE == MBG_LAYER_LIFT, last = MODE == MBG_LAYER_LAST;
+    constexpr int NG = lift ? NX : NGV;  // depth of the first ring
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int lrow = (warp & 3) * 32 + lane;  // tile row = TMEM lane
-    const int half = warp >> 2;               // columns 32 half .. +31 (64 half .. +63 of H)
     const uint32_t sb = (smem_u32(smem_raw) + 127u) & ~127u;
     uint8_t* const sbp = smem_raw + (sb - smem_u32(smem_raw));
     float* small = reinterpret_cast<float*>(sbp + OFF_SMALL);
-    const uint32_t mb_inv0 = smem_u32(&mbar[0]), mb_aux0 = smem_u32(&mbar[2]);
+    const uint32_t bar0 = smem_u32(&mbar[0]);
+    auto bar = [&](int k) { return bar0 + 8u * (uint32_t) k; };
+    volatile int* abort = &abort_sh;
     const int T = p.S / LT;
     const int nsamp = (p.batch - (int) blockIdx.x + (int) gridDim.x - 1) / (int) gridDim.x;
     const int n = nsamp * T;
-    const bool lift = p.mode == MBG_LAYER_LIFT, last = p.mode == MBG_LAYER_LAST;
+    auto sample = [&](int s) { return (int64_t) blockIdx.x + (int64_t) s * gridDim.x; };
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_sh)),
@@ -218,11 +193,19 @@ __global__ void __launch_bounds__(LNTH, 1) spectral_layer_kernel(const layer_par
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        for (int k = 0; k < 4; k++) mbar_init(smem_u32(&mbar[k]), 1);
+        for (int k = 0; k < NBAR; k++) {
+            uint32_t cnt = 1;
+            if (k == B_EACC || k == B_EACC + 1 || k == B_FOP || k == B_FOP + 1 || k == B_ED || k == B_ED + 1 ||
+                k == B_EH || k == B_EH + 1 || (lift && k >= B_EGV && k < B_EGV + NX))
+                cnt = NEPI / 32;  // one arrival per epilogue warp
+            mbar_init(bar(k), cnt);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        abort_sh = 0;
     }
     // per-CTA constants: bias, projection vectors (q2 in BF16, as a product
-    // operand), lifting weights (BF16-rounded, [feature][channel])
+    // operand), lifting weights (BF16-rounded, [feature][channel]); the
+    // dense weights' images
     for (int c = tid; c < 64; c += LNTH) small[SM_BIAS + c] = (p.bias && c < p.W) ? p.bias[c] : 0.0f;
     if (last) {
         for (int j = tid; j < 128; j += LNTH) {
@@ -235,212 +218,336 @@ __global__ void __launch_bounds__(LNTH, 1) spectral_layer_kernel(const layer_par
             const int f = e >> 6, c = e & 63;
             small[SM_P + e] = (f < p.Fi && c < p.W) ? bf16r(p.P[c * p.Fi + f]) : 0.0f;
         }
+    } else {
+        for (int e = tid; e < B_IMG / 16; e += LNTH) cp_async16(sb + OFF_W + e * 16, p.Wl + e * 8, 16u);
     }
-    // copy groups: the once-per-CTA tiles with tile 0, then tile 1's
-    // per-sample operands; iteration t commits tile t+1's shared operands,
-    // then tile t+2's per-sample ones
-    if (!lift) {
-        for (int e = tid; e < 512; e += LNTH) {
-            const int o = e >> 3, kc = e & 7;
-            const bool ok = o < p.W && kc * 8 < p.W;
-            cp_async16(sb + OFF_W + koff(o, kc, 8), ok ? p.Wl + (int64_t) o * p.W + kc * 8 : p.Wl, ok ? 16u : 0u);
-        }
-    }
-    if (last) {
-        for (int e = tid; e < 1024; e += LNTH) {
-            const int j = e >> 3, kc = e & 7;
-            const bool ok = j < p.Hq && kc * 8 < p.W;
-            cp_async16(sb + OFF_Q + koff(j, kc, 8), ok ? p.Q1 + (int64_t) j * p.W + kc * 8 : p.Q1, ok ? 16u : 0u);
-        }
-    }
-    if (n > 0) {
-        copy_shared_ops(p, 0, T, sb, tid);
-        copy_sample_ops(p, 0, T, sb, tid);
-    }
-    cp_async_commit();
-    if (n > 1) copy_sample_ops(p, 1, T, sb, tid);
-    cp_async_commit();
+    if (last)
+        for (int e = tid; e < IMG / 16; e += LNTH) cp_async16(sb + OFF_Q + e * 16, p.Q1 + e * 8, 16u);
+    if (!lift)  // the Y images' padding (rows o >= W, K >= 2 Mo) is never written again
+        for (int e = tid; e < NYR * B_IMG / 16; e += LNTH)
+            st_shared_v4(sb + OFF_Y + (uint32_t) (e * 16), 0u, 0u, 0u, 0u);
+    cp_async_wait_all();
+    fence_async_smem();
     fence_before();
     __syncthreads();
     fence_after();
     const uint32_t tmem = tmem_sh;
-    const uint32_t tlane = (uint32_t) ((warp & 3) * 32) << 16;
-    const int nk1 = (2 * p.Mo + 15) / 16, nk2 = (p.W + 15) / 16;
 
-    bool fail = false;
-    for (int t = 0; t <= n + 2; t++) {
-        // tile t's operands have landed (only tile t+1's per-sample copies may be in flight)
-        if (t < n) {
-            cp_async_wait<1>();
-            fence_async_smem();
-        }
-        if (__syncthreads_or(fail)) {
-            fail = true;
-            break;
-        }
-        // first product of tile t into accumulator t % 2
-        if (t < n && !lift && tid == 0) {
-            fence_after();
-            const uint32_t sg = sb + OFF_G + (uint32_t) ((t % NG) * A_TILE);
-            const uint32_t sv = sb + OFF_V + (uint32_t) ((t % NV) * A_TILE);
-            const uint32_t sy = sb + OFF_Y + (uint32_t) (((t / T) % NY) * B_TILE), sw = sb + OFF_W;
-            const uint32_t d = tmem + (uint32_t) ((t & 1) * 64);
-            for (int kk = 0; kk < nk1; kk++)
-                mma_bf16(d, smem_desc_nsw(sg + kk * 256, 128, 1024), smem_desc_nsw(sy + kk * 256, 128, 1024), ID64,
-                         kk > 0 ? 1u : 0u);
-            for (int kk = 0; kk < nk2; kk++)
-                mma_bf16(d, smem_desc_nsw(sv + kk * 256, 128, 1024), smem_desc_nsw(sw + kk * 256, 128, 1024), ID64,
-                         1u);
-            mma_commit(mb_inv0 + 8u * (uint32_t) (t & 1));
-        }
-        // first product of tile t-1 and second product of tile t-3 done
-        if (t >= 1 && t <= n && !lift && !mbar_wait(mb_inv0 + 8u * (uint32_t) ((t - 1) & 1), ((t - 1) >> 1) & 1))
-            fail = true;
-        if (t >= 3 && !mbar_wait(mb_aux0 + 8u * (uint32_t) ((t - 3) & 1), ((t - 3) >> 1) & 1)) fail = true;
-        fail = __any_sync(0xFFFFFFFFu, fail);  // warp-uniform: the TMEM loads below are warp-wide
-        fence_after();
-        // copies (their ring slots were last read by the products just waited for)
-        if (!fail && t + 1 < n) copy_shared_ops(p, t + 1, T, sb, tid);
-        cp_async_commit();
-        if (!fail && t + 2 < n) copy_sample_ops(p, t + 2, T, sb, tid);
-        cp_async_commit();
-
-        // second product of tile t-3: a finished sample's spectrum, or y
-        float ysum = 0.0f;
-        if (!fail && t >= 3) {
-            const int u = t - 3;
-            if (last) {
+    if (warp == PROD_WARP) {
+        // ---------------------------------------------------------- copies
+        // Two queues, each served as soon as its next slot is free: tile
+        // ug's (G, v) pair (LIFT: its X tile), with the sample's mixed
+        // spectrum Y at a sample's first tile; tile uf's DFT-basis tile
+        // (after tile uf's pair). Lane 0 polls; the warp follows.
+        int ug = 0, uf = last ? n : 0;
+        uint32_t idle = 0;
+        while (ug < n || uf < n) {
+            int did = 0;
+            if (ug < n) {
+                const int s = ug / T, i = ug % T, g = ug % NG;
+                const bool needy = !lift && i == 0;
+                int ok = 0;
+                if (lane == 0)
+                    ok = mbar_peek(bar(B_EGV + g), ((ug / NG) & 1) ^ 1) &&
+                        (!needy || mbar_peek(bar(B_EY + s % NYR), ((s / NYR) & 1) ^ 1));
+                if (__shfl_sync(0xFFFFFFFFu, ok, 0)) {
+                    const int64_t b = sample(s);
+                    if (lane == 0) {
+                        if (lift) {
+                            const uint32_t bytes = (uint32_t) (LT * p.Fi * 4);
+                            mbar_arrive_tx(bar(B_FGV + g), bytes);
+                            bulk_g2s(sb + OFF_GV + (uint32_t) (g * X_SLOT), p.X + (b * p.S + (int64_t) i * LT) * p.Fi,
+                                     bytes, bar(B_FGV + g));
+                        } else {
+                            const uint32_t dst = sb + OFF_GV + (uint32_t) (g * GV_SLOT);
+                            mbar_arrive_tx(bar(B_FGV + g), 2 * IMG);
+                            bulk_g2s(dst, p.G + (int64_t) i * IMG_ELEMS, IMG, bar(B_FGV + g));
+                            bulk_g2s(dst + IMG, p.v + (b * T + i) * IMG_ELEMS, IMG, bar(B_FGV + g));
+                        }
+                    }
+                    if (needy) {
+                        // the sample's mixed spectrum [2 Mo][W] transposed into the B
+                        // image (rows o, K = [Re | Im] modes); entries beyond W, 2 Mo
+                        // stay zero
+                        const int ys = s % NYR;
+                        const uint32_t dy = sb + OFF_Y + (uint32_t) (ys * B_IMG);
+                        const int wc = p.W / 8, nch = 2 * p.Mo * wc;  // <= 512 chunks of 8 channels
 #pragma unroll 1
-                for (int q = 0; q < 4; q++) {
-                    float h[16];
-                    tmem_ld16(tmem + tlane + 256u + (uint32_t) ((u & 1) * 128 + half * 64 + q * 16), h);
+                        for (int t0 = 0; t0 < 16; t0 += 8) {  // 8 loads in flight per lane
+                            uint4 q[8];
 #pragma unroll
-                    for (int k = 0; k < 16; k++) {
-                        const int j = half * 64 + q * 16 + k;
-                        const float z = bf16r(gelu(h[k] + small[SM_BQ1 + j]));
-                        ysum = fmaf(z, small[SM_Q2 + j], ysum);
-                    }
-                }
-                if (half == 1) small[SM_RED + lrow] = ysum;
-            } else if (u % T == T - 1 && (warp & 3) < 2) {
-                float d0[16], d1[16];
-                const uint32_t ta = tmem + tlane + 128u + (uint32_t) (((u / T) & 1) * 64 + half * 32);
-                tmem_ld16(ta, d0);
-                tmem_ld16(ta + 16u, d1);
-                if (lrow < 2 * p.Mo) {
-                    __nv_bfloat16* dst = p.vhT + (tile_sample(u, T) * 2 * p.Mo + lrow) * p.W + half * 32;
+                            for (int t = 0; t < 8; t++) {
+                                const int e = lane + 32 * (t0 + t), m = e / wc, o0 = (e % wc) * 8;
+                                if (e < nch)
+                                    q[t] = *reinterpret_cast<const uint4*>(p.Y + (b * 2 * p.Mo + m) * p.W + o0);
+                            }
 #pragma unroll
-                    for (int c8 = 0; c8 < 4; c8++) {
-                        if (half * 32 + c8 * 8 >= p.W) break;
-                        const float* s8 = c8 < 2 ? d0 + c8 * 8 : d1 + (c8 - 2) * 8;
-                        *reinterpret_cast<uint4*>(dst + c8 * 8) =
-                            make_uint4(pack_bf16(s8[0], s8[1]), pack_bf16(s8[2], s8[3]), pack_bf16(s8[4], s8[5]),
-                                       pack_bf16(s8[6], s8[7]));
+                            for (int t = 0; t < 8; t++) {
+                                const int e = lane + 32 * (t0 + t), m = e / wc, o0 = (e % wc) * 8;
+                                if (e >= nch) break;
+                                const uint32_t w[4] = {q[t].x, q[t].y, q[t].z, q[t].w};
+                                const uint32_t base = dy + (uint32_t) ((m >> 3) * 128 + (m & 7) * 2);
+#pragma unroll
+                                for (int k = 0; k < 8; k++) {
+                                    const int o = o0 + k;
+                                    st_shared_u16(base + (uint32_t) ((o >> 3) * 1024 + (o & 7) * 16),
+                                                  (k & 1) ? (w[k >> 1] >> 16) : (w[k >> 1] & 0xFFFFu));
+                                }
+                            }
+                        }
+                        fence_async_smem();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(bar(B_FY + ys));
                     }
+                    ug++;
+                    did = 1;
                 }
             }
+            if (uf < ug) {
+                const int f = uf % NFR;
+                int ok = 0;
+                if (lane == 0) ok = mbar_peek(bar(B_EF + f), ((uf / NFR) & 1) ^ 1);
+                if (__shfl_sync(0xFFFFFFFFu, ok, 0)) {
+                    if (lane == 0) {
+                        mbar_arrive_tx(bar(B_FF + f), F_IMG);
+                        bulk_g2s(sb + OFF_F + (uint32_t) (f * F_IMG), p.F + (int64_t) (uf % T) * IMG_ELEMS, F_IMG,
+                                 bar(B_FF + f));
+                    }
+                    uf++;
+                    did = 1;
+                }
+            }
+            int stop = 0;
+            if (lane == 0) {
+                idle = did ? 0 : idle + 1;
+                if (idle >= WAIT_LIMIT) *abort = 1;
+                stop = *abort;
+                if (!did) __nanosleep(32);
+            }
+            if (__shfl_sync(0xFFFFFFFFu, stop, 0)) break;
         }
-
-        // epilogue of tile t-1
-        if (!fail && t >= 1 && t <= n) {
-            const int u = t - 1;
-            const int64_t grow = tile_sample(u, T) * p.S + (int64_t) (u % T) * LT + lrow;
-            float x[32];
-            if (lift) {
-                const float* xs = reinterpret_cast<const float*>(sbp + OFF_X + (u % NX) * X_TILE) + lrow * p.Fi;
+    } else if (warp == MMA_WARP) {
+        // ---------------------------------------------------------- MMAs
+        // Two queues, each issued as soon as its operands and accumulator are
+        // ready: tile ui's first product, tile ud's second product (after
+        // tile ud's first).
+        if (lane == 0) {
+            const int nk1 = (2 * p.Mo + 15) / 16, nk2 = (p.W + 15) / 16;
+            int ui = lift ? n : 0, ud = 0;
+            uint32_t idle = 0;
+            while (ud < n) {
+                bool did = false;
+                if (ui < n) {
+                    const int s = ui / T, i = ui % T, g = ui % NG;
+                    if (mbar_peek(bar(B_FGV + g), (ui / NG) & 1) &&
+                        (i != 0 || mbar_peek(bar(B_FY + s % NYR), (s / NYR) & 1)) &&
+                        mbar_peek(bar(B_EACC + (ui & 1)), ((ui >> 1) & 1) ^ 1)) {
+                        fence_after();
+                        const uint32_t sg = sb + OFF_GV + (uint32_t) (g * GV_SLOT), sv = sg + IMG;
+                        const uint32_t sy = sb + OFF_Y + (uint32_t) ((s % NYR) * B_IMG), sw = sb + OFF_W;
+                        const uint32_t d = tmem + (uint32_t) ((ui & 1) * 64);
+                        for (int kk = 0; kk < nk1; kk++)
+                            mma_bf16(d, smem_desc_nsw(sg + kk * 256, 128, 1024),
+                                     smem_desc_nsw(sy + kk * 256, 128, 1024), ID64, kk > 0 ? 1u : 0u);
+                        for (int kk = 0; kk < nk2; kk++)
+                            mma_bf16(d, smem_desc_nsw(sv + kk * 256, 128, 1024),
+                                     smem_desc_nsw(sw + kk * 256, 128, 1024), ID64, 1u);
+                        mma_commit(bar(B_FACC + (ui & 1)));
+                        mma_commit(bar(B_EGV + g));
+                        if (i == T - 1) mma_commit(bar(B_EY + s % NYR));
+                        ui++;
+                        did = true;
+                    }
+                }
+                if (ud < ui) {
+                    const int w = ud, sw = w / T, iw = w % T;
+                    if (last) {
+                        if (mbar_peek(bar(B_FOP + (w & 1)), (w >> 1) & 1) &&
+                            mbar_peek(bar(B_EH + (w & 1)), ((w >> 1) & 1) ^ 1)) {
+                            fence_after();
+                            const uint32_t so = sb + OFF_VT + (uint32_t) ((w & 1) * VT_IMG);
+                            for (int kk = 0; kk < nk2; kk++)
+                                mma_bf16(tmem + 256u + (uint32_t) ((w & 1) * 128),
+                                         smem_desc_nsw(so + kk * 256, 128, 1024),
+                                         smem_desc_nsw(sb + OFF_Q + kk * 256, 128, 1024), ID128, kk > 0 ? 1u : 0u);
+                            mma_commit(bar(B_EOP + (w & 1)));
+                            mma_commit(bar(B_FH + (w & 1)));
+                            ud++;
+                            did = true;
+                        }
+                    } else {
+                        const int f = w % NFR;
+                        if (mbar_peek(bar(B_FOP + (w & 1)), (w >> 1) & 1) && mbar_peek(bar(B_FF + f), (w / NFR) & 1) &&
+                            (iw != 0 || mbar_peek(bar(B_ED + (sw & 1)), ((sw >> 1) & 1) ^ 1))) {
+                            fence_after();
+                            const uint32_t sf = sb + OFF_F + (uint32_t) (f * F_IMG);
+                            const uint32_t d = tmem + 128u + (uint32_t) ((sw & 1) * 64);
 #pragma unroll
-                for (int j = 0; j < 32; j++) x[j] = 0.0f;
+                            for (int kk = 0; kk < LT / 16; kk++)
+                                mma_bf16(d, smem_desc_nsw(sf + kk * 256, 128, 2048),
+                                         smem_desc_nsw(sb + OFF_VT + (uint32_t) ((w & 1) * VT_IMG) + kk * 2 * VT_LBO,
+                                                       VT_LBO, VT_SBO),
+                                         ID64, (iw != 0 || kk > 0) ? 1u : 0u);
+                            mma_commit(bar(B_EOP + (w & 1)));
+                            mma_commit(bar(B_EF + f));
+                            if (iw == T - 1) mma_commit(bar(B_FD + (sw & 1)));
+                            ud++;
+                            did = true;
+                        }
+                    }
+                }
+                idle = did ? 0 : idle + 1;
+                if (idle >= WAIT_LIMIT) *abort = 1;
+                if (*abort) break;
+                if (!did) __nanosleep(32);
+            }
+        }
+    } else {
+        // ---------------------------------------------------------- epilogues
+        const int lrow = (warp & 3) * 32 + lane;  // tile row = TMEM lane
+        const int qt = warp >> 2;                 // columns 16 qt .. +15 (32 qt .. +31 of H)
+        const uint32_t tlane = (uint32_t) ((warp & 3) * 32) << 16;
+
+        // a finished sample's spectrum: D rows = modes (lanes 0..63)
+        auto readout = [&](int sr) {
+            wait_bar_warp(bar(B_FD + (sr & 1)), (sr >> 1) & 1, abort, lane);
+            fence_after();
+            if ((warp & 3) < 2) {
+                float d[16];
+                tmem_ld16(tmem + tlane + 128u + (uint32_t) ((sr & 1) * 64 + qt * 16), d);
+                if (lrow < 2 * p.Mo) {
+                    __nv_bfloat16* dst = p.vhT + (sample(sr) * 2 * p.Mo + lrow) * p.W + qt * 16;
+#pragma unroll
+                    for (int c8 = 0; c8 < 2; c8++)
+                        if (qt * 16 + c8 * 8 < p.W)
+                            *reinterpret_cast<uint4*>(dst + c8 * 8) =
+                                make_uint4(pack_bf16(d[8 * c8], d[8 * c8 + 1]), pack_bf16(d[8 * c8 + 2], d[8 * c8 + 3]),
+                                           pack_bf16(d[8 * c8 + 4], d[8 * c8 + 5]),
+                                           pack_bf16(d[8 * c8 + 6], d[8 * c8 + 7]));
+                }
+            }
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bar(B_ED + (sr & 1)));
+        };
+        // a tile's output: the column quarters' GELU(H + bq1) . q2 sums
+        auto project = [&](int w) {
+            wait_bar_warp(bar(B_FH + (w & 1)), (w >> 1) & 1, abort, lane);
+            fence_after();
+            float ysum = 0.0f;
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                float h[16];
+                tmem_ld16(tmem + tlane + 256u + (uint32_t) ((w & 1) * 128 + qt * 32 + q * 16), h);
+#pragma unroll
+                for (int k = 0; k < 16; k++) {
+                    const int j = qt * 32 + q * 16 + k;
+                    const float z = bf16r(gelu(h[k] + small[SM_BQ1 + j]));
+                    ysum = fmaf(z, small[SM_Q2 + j], ysum);
+                }
+            }
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bar(B_EH + (w & 1)));
+            float* red = small + SM_RED + (w & 1) * 512;
+            red[qt * 128 + lrow] = ysum;
+            named_sync(3, NEPI);
+            if (qt == 0)
+                p.y[sample(w / T) * p.S + (int64_t) (w % T) * LT + lrow] =
+                    ((red[lrow] + red[128 + lrow]) + (red[256 + lrow] + red[384 + lrow])) + p.bq2[0];
+        };
+
+        for (int u = 0; u < n; u++) {
+            const int s = u / T, i = u % T;
+            float x[16];
+            if (lift) {
+                const int g = u % NX;
+                wait_bar_warp(bar(B_FGV + g), (u / NX) & 1, abort, lane);
+                const float* xs = reinterpret_cast<const float*>(sbp + OFF_GV + g * X_SLOT) + lrow * p.Fi;
+#pragma unroll
+                for (int j = 0; j < 16; j++) x[j] = 0.0f;
                 for (int f = 0; f < p.Fi; f++) {
                     const float xv = bf16r(xs[f]);
-                    const float4* w4 = reinterpret_cast<const float4*>(small + SM_P + f * 64 + half * 32);
+                    const float4* w4 = reinterpret_cast<const float4*>(small + SM_P + f * 64 + qt * 16);
 #pragma unroll
-                    for (int q = 0; q < 8; q++) {
-                        const float4 w = w4[q];
-                        x[4 * q] = fmaf(xv, w.x, x[4 * q]);
-                        x[4 * q + 1] = fmaf(xv, w.y, x[4 * q + 1]);
-                        x[4 * q + 2] = fmaf(xv, w.z, x[4 * q + 2]);
-                        x[4 * q + 3] = fmaf(xv, w.w, x[4 * q + 3]);
+                    for (int q = 0; q < 4; q++) {
+                        const float4 wq = w4[q];
+                        x[4 * q] = fmaf(xv, wq.x, x[4 * q]);
+                        x[4 * q + 1] = fmaf(xv, wq.y, x[4 * q + 1]);
+                        x[4 * q + 2] = fmaf(xv, wq.z, x[4 * q + 2]);
+                        x[4 * q + 3] = fmaf(xv, wq.w, x[4 * q + 3]);
                     }
                 }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bar(B_EGV + g));
             } else {
-                float a0[16], a1[16];
-                const uint32_t ta = tmem + tlane + (uint32_t) ((u & 1) * 64 + half * 32);
-                tmem_ld16(ta, a0);
-                tmem_ld16(ta + 16u, a1);
-#pragma unroll
-                for (int j = 0; j < 16; j++) {
-                    x[j] = a0[j];
-                    x[16 + j] = a1[j];
-                }
+                wait_bar_warp(bar(B_FACC + (u & 1)), (u >> 1) & 1, abort, lane);
+                fence_after();
+                tmem_ld16(tmem + tlane + (uint32_t) ((u & 1) * 64 + qt * 16), x);
+                fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bar(B_EACC + (u & 1)));
             }
-            uint32_t pk[16];
+            uint32_t pk[8];
 #pragma unroll
-            for (int j = 0; j < 32; j += 2) {
-                float v0 = x[j] + small[SM_BIAS + half * 32 + j];
-                float v1 = x[j + 1] + small[SM_BIAS + half * 32 + j + 1];
-                if (p.act == MBG_ACT_GELU) {
+            for (int j = 0; j < 16; j += 2) {
+                float v0 = x[j] + small[SM_BIAS + qt * 16 + j];
+                float v1 = x[j + 1] + small[SM_BIAS + qt * 16 + j + 1];
+                if (GELU) {
                     v0 = gelu(v0);
                     v1 = gelu(v1);
                 }
                 pk[j >> 1] = pack_bf16(v0, v1);
             }
-            const uint32_t so = sb + OFF_VT + (uint32_t) ((u & 1) * VT_TILE);
             if (!last) {
-                __nv_bfloat16* dst = p.v_out + grow * p.W + half * 32;
+                // the output image (free once the bulk store of tile u-1 has read it)
+                const uint32_t so = sb + OFF_OUT;
+                if (tid == 0) bulk_wait_read<0>();
+                named_sync(1, NEPI);
 #pragma unroll
-                for (int c8 = 0; c8 < 4; c8++)
-                    if (half * 32 + c8 * 8 < p.W)
-                        *reinterpret_cast<uint4*>(dst + c8 * 8) =
-                            make_uint4(pk[4 * c8], pk[4 * c8 + 1], pk[4 * c8 + 2], pk[4 * c8 + 3]);
-                // element (channel c, sample lrow) of the transposed tile
-                const uint32_t tb = so + (uint32_t) (lrow >> 3) * VT_LBO + (uint32_t) (lrow & 7) * 2;
+                for (int c8 = 0; c8 < 2; c8++)
+                    st_shared_v4(so + koff(lrow, qt * 2 + c8, 8), pk[4 * c8], pk[4 * c8 + 1], pk[4 * c8 + 2],
+                                 pk[4 * c8 + 3]);
+                // transposed tile u % 2 (free once the DFT of tile u-2 is done)
+                wait_bar_warp(bar(B_EOP + (u & 1)), ((u >> 1) & 1) ^ 1, abort, lane);
+                const uint32_t tb = sb + OFF_VT + (uint32_t) ((u & 1) * VT_IMG) + (uint32_t) (lrow >> 3) * VT_LBO +
+                    (uint32_t) (lrow & 7) * 2;
 #pragma unroll
-                for (int j = 0; j < 32; j++) {
-                    const int c = half * 32 + j;
+                for (int j = 0; j < 16; j++) {
+                    const int c = qt * 16 + j;
                     st_shared_u16(tb + (uint32_t) (c >> 3) * VT_SBO + (uint32_t) (c & 7) * 16,
                                   (j & 1) ? (pk[j >> 1] >> 16) : (pk[j >> 1] & 0xFFFFu));
                 }
+                fence_async_smem();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bar(B_FOP + (u & 1)));
+                named_sync(2, NEPI);
+                if (tid == 0) {
+                    bulk_s2g(p.v_out + (sample(s) * T + i) * IMG_ELEMS, so, IMG);
+                    bulk_commit();
+                }
+                if (i == 0 && s >= 1) readout(s - 1);
             } else {
+                // the projection's input image (free once the projection of tile u-2 is done)
+                wait_bar_warp(bar(B_EOP + (u & 1)), ((u >> 1) & 1) ^ 1, abort, lane);
+                const uint32_t so = sb + OFF_VT + (uint32_t) ((u & 1) * VT_IMG);
 #pragma unroll
-                for (int c8 = 0; c8 < 4; c8++)
-                    st_shared_v4(so + koff(lrow, half * 4 + c8, 8), pk[4 * c8], pk[4 * c8 + 1], pk[4 * c8 + 2],
+                for (int c8 = 0; c8 < 2; c8++)
+                    st_shared_v4(so + koff(lrow, qt * 2 + c8, 8), pk[4 * c8], pk[4 * c8 + 1], pk[4 * c8 + 2],
                                  pk[4 * c8 + 3]);
+                fence_async_smem();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bar(B_FOP + (u & 1)));
+                if (u >= 1) project(u - 1);
             }
         }
-        fence_async_smem();
-        fence_before();
-        if (__syncthreads_or(fail)) {
-            fail = true;
-            break;
+        if (n > 0) {
+            if (!last) readout(nsamp - 1);
+            else project(n - 1);
         }
-        // output of tile t-3 (the two column halves' partial sums)
-        if (last && t >= 3 && half == 0) {
-            const int u = t - 3;
-            p.y[tile_sample(u, T) * p.S + (int64_t) (u % T) * LT + lrow] = (ysum + small[SM_RED + lrow]) + p.bq2[0];
-        }
-        // second product of tile t-1
-        if (t >= 1 && t <= n && tid == 0) {
-            fence_after();
-            const int u = t - 1;
-            const uint32_t so = sb + OFF_VT + (uint32_t) ((u & 1) * VT_TILE);
-            if (last) {
-                for (int kk = 0; kk < nk2; kk++)
-                    mma_bf16(tmem + 256u + (uint32_t) ((u & 1) * 128), smem_desc_nsw(so + kk * 256, 128, 1024),
-                             smem_desc_nsw(sb + OFF_Q + kk * 256, 128, 1024), ID128, kk > 0 ? 1u : 0u);
-            } else {
-                const uint32_t sf = sb + OFF_F + (uint32_t) ((u % NF) * F_TILE);
-                const uint32_t d = tmem + 128u + (uint32_t) (((u / T) & 1) * 64);
-#pragma unroll
-                for (int kk = 0; kk < LT / 16; kk++)
-                    mma_bf16(d, smem_desc_nsw(sf + kk * 256, 128, 2048),
-                             smem_desc_nsw(so + kk * 2 * VT_LBO, VT_LBO, VT_SBO), ID64,
-                             (u % T != 0 || kk > 0) ? 1u : 0u);
-            }
-            mma_commit(mb_aux0 + 8u * (uint32_t) (u & 1));
-        }
+        if (tid == 0) bulk_wait<0>();
     }
-    cp_async_wait<0>();
-    if (fail && tid == 0) atomicOr(p.status, ST_WAIT);
+    if (tid == 0 && abort_sh) atomicOr(p.status, ST_WAIT);
     fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -509,10 +616,32 @@ void spectral_layer(const mbg_fno_layer_desc* d, cudaStream_t s)
         throw std::runtime_error("CUDA: device query failed");
     static std::once_flag attr;
     std::call_once(attr, [] {
-        cudaFuncSetAttribute(spectral_layer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, LAYER_SMEM);
+        const void* ks[] = {(const void*) spectral_layer_kernel<MBG_LAYER_LIFT, false>,
+                            (const void*) spectral_layer_kernel<MBG_LAYER_LIFT, true>,
+                            (const void*) spectral_layer_kernel<MBG_LAYER_MID, false>,
+                            (const void*) spectral_layer_kernel<MBG_LAYER_MID, true>,
+                            (const void*) spectral_layer_kernel<MBG_LAYER_LAST, false>,
+                            (const void*) spectral_layer_kernel<MBG_LAYER_LAST, true>};
+        for (const void* k : ks) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, LAYER_SMEM);
     });
     const int grid = d->batch < sms ? d->batch : sms;
-    spectral_layer_kernel<<<grid, LNTH, LAYER_SMEM, s>>>(p);
+    const bool g = d->act == MBG_ACT_GELU;
+    if (d->mode == MBG_LAYER_LIFT) {
+        if (g)
+            spectral_layer_kernel<MBG_LAYER_LIFT, true><<<grid, LNTH, LAYER_SMEM, s>>>(p);
+        else
+            spectral_layer_kernel<MBG_LAYER_LIFT, false><<<grid, LNTH, LAYER_SMEM, s>>>(p);
+    } else if (d->mode == MBG_LAYER_MID) {
+        if (g)
+            spectral_layer_kernel<MBG_LAYER_MID, true><<<grid, LNTH, LAYER_SMEM, s>>>(p);
+        else
+            spectral_layer_kernel<MBG_LAYER_MID, false><<<grid, LNTH, LAYER_SMEM, s>>>(p);
+    } else {
+        if (g)
+            spectral_layer_kernel<MBG_LAYER_LAST, true><<<grid, LNTH, LAYER_SMEM, s>>>(p);
+        else
+            spectral_layer_kernel<MBG_LAYER_LAST, false><<<grid, LNTH, LAYER_SMEM, s>>>(p);
+    }
     check_launch("spectral_layer_kernel");
 }
 

@@ -114,6 +114,7 @@ class FNO:
         self._ibufs = {}
         self._blk_valid = False
         self._wb = {}   # BF16 copies of the dense weights (inference)
+        self._img = {}  # BF16 tile images for the fused layer kernel
 
     # ------------------------------------------------------------ helpers
     def _views(self, flat):
@@ -164,6 +165,8 @@ class FNO:
                 w = self._wb[name] = torch.empty(self.p[name].numel(), dtype=torch.bfloat16,
                                                  device=self.dev)
             K.cast_bf16(self.p[name], w)
+        if self.fused_ok():
+            self._layer_images()
         self._blk_valid = True
 
     @staticmethod
@@ -247,6 +250,30 @@ class FNO:
         return (sh.S % 128 == 0 and sh.W <= 64 and 2 * sh.Mo <= 64
                 and sh.Hq <= 128 and sh.F <= 16)
 
+    def _layer_images(self):
+        """BF16 tile images for the fused layer kernel: the DFT bases (once)
+        and the dense weights (after every parameter change)."""
+        sh = self.sh
+        S, W, Mo, Hq = sh.S, sh.W, sh.Mo, sh.Hq
+        T, b16, d = S // 128, torch.bfloat16, self.dev
+        im = self._img
+        if "G" not in im:
+            F, G = dft_bases(S, Mo)
+            F32 = torch.tensor(F, dtype=torch.float32, device=d)
+            G32 = torch.tensor(G, dtype=torch.float32, device=d)
+            im["G"] = torch.empty(T * 8192, dtype=b16, device=d)
+            im["F"] = torch.empty(T * 8192, dtype=b16, device=d)
+            K.image_bf16(G32, T, 128, 2 * Mo, 2 * Mo, 128 * 2 * Mo, 128, 64, im["G"])
+            K.image_bf16(F32, T, 2 * Mo, 128, S, 128, 64, 128, im["F"])
+        for l in range(sh.L):
+            name = "W%d" % l
+            if name not in im:
+                im[name] = torch.empty(64 * 64, dtype=b16, device=d)
+            K.image_bf16(self.p[name], 1, W, W, W, 0, 64, 64, im[name])
+        if "Q1" not in im:
+            im["Q1"] = torch.empty(128 * 64, dtype=b16, device=d)
+        K.image_bf16(self.p["Q1"], 1, Hq, W, W, 0, 128, 64, im["Q1"])
+
     def _fbuffers(self, B):
         key = ("fused", B)
         if key in self._ibufs:
@@ -255,7 +282,7 @@ class FNO:
         S, W, Mo = sh.S, sh.W, sh.Mo
         b16 = torch.bfloat16
         b = dict(
-            v=[torch.empty(B * S * W, dtype=b16, device=d) for _ in range(2)],
+            v=[torch.empty(B * S * 64, dtype=b16, device=d) for _ in range(2)],
             VhT=torch.empty(B * 2 * Mo * W, dtype=b16, device=d),
             Y=torch.empty(B * 2 * W * Mo, dtype=b16, device=d),
             y=torch.empty(B * S, dtype=torch.float32, device=d))
@@ -269,10 +296,12 @@ class FNO:
         one launch that keeps its products on chip: the lifting with the
         first truncated DFT; the inverse DFT, pointwise mix, bias and GELU
         with the next DFT; the last layer with the projection and the
-        output layer. Between them one product per layer mixes the modes
-        of all samples (M = batch, N = 2 W, per mode), writing the mixed
-        spectrum as BF16 [B, 2, W, Mo]. Otherwise the products of
-        _infer_products run. X: FP32 [B, S, F]; returns y [B, S] (a view of
+        output layer. Between them two products per layer mix the modes of
+        all samples (M = batch, N = W, per mode; the Re and the Im outputs),
+        writing the mixed spectrum as BF16 [B, 2, Mo, W]. Activations pass between the fused
+        launches as BF16 tile images (the layout their products read), the
+        DFT bases and dense weights likewise (_layer_images). Otherwise the
+        products of _infer_products run. X: FP32 [B, S, F]; returns y [B, S] (a view of
         an internal buffer)."""
         sh = self.sh
         S, W, Mo, L, Fi, Hq = sh.S, sh.W, sh.Mo, sh.L, sh.F, sh.Hq
@@ -286,30 +315,34 @@ class FNO:
         p = self.p
         if not self._blk_valid:
             self._mode_blocks()
-        wb = self._wb
+        im = self._img
         vhT, Y = b["VhT"], b["Y"]
         K.spectral_layer(T.MBG_LAYER_LIFT, T.MBG_ACT_NONE, B, S, W, Mo, Fi=Fi,
                          X=X, P=p["P"], bias=p["bp"], v_out=b["v"][0],
-                         F=self.F, vhT=vhT)
+                         F=im["F"], vhT=vhT)
         cur = 0
         for l in range(L):
-            # mode mixing, per mode m: Y[b, :, :, m] = blk[m] [Re; Im]
+            # mode mixing per mode m, the Re and the Im outputs:
+            # Y[b, part, m, :] = blk[m][part] [Re; Im] (contiguous stores)
             blk = self.blk[l]
-            K.gemm(B, 2 * W,
-                   [Seg(vhT, 0, 2 * Mo * W, 1, W, blk, 0, 2 * W, 1, 4 * W * W, W),
-                    Seg(vhT, Mo * W, 2 * Mo * W, 1, W, blk, W, 2 * W, 1, 4 * W * W, W)],
-                   Y, 0, 2 * W * Mo, Mo, 1, batch=Mo)
+            for part in range(2):
+                K.gemm(B, W,
+                       [Seg(vhT, 0, 2 * Mo * W, 1, W, blk, part * W * 2 * W,
+                            2 * W, 1, 4 * W * W, W),
+                        Seg(vhT, Mo * W, 2 * Mo * W, 1, W, blk,
+                            part * W * 2 * W + W, 2 * W, 1, 4 * W * W, W)],
+                       Y, part * Mo * W, 2 * Mo * W, 1, W, batch=Mo)
             if l < L - 1:
                 K.spectral_layer(T.MBG_LAYER_MID, T.MBG_ACT_GELU, B, S, W, Mo,
-                                 v=b["v"][cur], Y=Y, G=self.G, Wl=wb["W%d" % l],
+                                 v=b["v"][cur], Y=Y, G=im["G"], Wl=im["W%d" % l],
                                  bias=p["bw%d" % l], v_out=b["v"][1 - cur],
-                                 F=self.F, vhT=vhT)
+                                 F=im["F"], vhT=vhT)
                 cur = 1 - cur
             else:
                 K.spectral_layer(T.MBG_LAYER_LAST, T.MBG_ACT_NONE, B, S, W, Mo,
-                                 Hq=Hq, v=b["v"][cur], Y=Y, G=self.G,
-                                 Wl=wb["W%d" % l], bias=p["bw%d" % l],
-                                 Q1=wb["Q1"], bq1=p["bq1"], q2=p["q2"],
+                                 Hq=Hq, v=b["v"][cur], Y=Y, G=im["G"],
+                                 Wl=im["W%d" % l], bias=p["bw%d" % l],
+                                 Q1=im["Q1"], bq1=p["bq1"], q2=p["q2"],
                                  bq2=p["bq2"], y=b["y"])
         return b["y"].view(B, S)
 

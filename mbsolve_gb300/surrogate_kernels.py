@@ -123,26 +123,28 @@ def spectral_layer(mode, act, batch, S, W, Mo, Fi=0, Hq=0, X=None, P=None,
                    y=None):
     """One Fourier layer of inference in one launch (mbg_fno_spectral_layer):
     mode MBG_LAYER_LIFT (X [B, S, Fi], P [W, Fi] FP32), MBG_LAYER_MID (v
-    [B, S, W], Y [B, 2, W, Mo], G [S, 2 Mo], Wl [W, W] BF16) or
-    MBG_LAYER_LAST (the same plus Q1 [Hq, W] BF16, bq1, q2 [Hq], bq2 [1]
-    FP32, y [B, S] FP32); LIFT and MID write v_out [B, S, W] and the
-    spectrum vhT [B, 2 Mo, W] (BF16) with F [2 Mo, S] BF16."""
-    B = int(batch)
+    activation images [B S 64], Y [B, 2, Mo, W], G images [S/128, 8192],
+    Wl image [64 64], BF16) or MBG_LAYER_LAST (the same plus the Q1 image
+    [128 64] BF16, bq1, q2 [Hq], bq2 [1] FP32 and y [B, S] FP32); LIFT and
+    MID write the activation images v_out [B S 64] and the spectrum vhT
+    [B, 2 Mo, W] (BF16) with the F images [S/128, 8192]. Images as
+    written by image_bf16 (include/mbsolve_fno.h)."""
+    B, ntile = int(batch), int(S) // 128
     need = {}
     if mode == T.MBG_LAYER_LIFT:
         need.update(X=(X, torch.float32, B * S * Fi), P=(P, torch.float32, W * Fi))
     else:
-        need.update(v=(v, torch.bfloat16, B * S * W),
+        need.update(v=(v, torch.bfloat16, B * S * 64),
                     Y=(Y, torch.bfloat16, B * 2 * W * Mo),
-                    G=(G, torch.bfloat16, S * 2 * Mo),
-                    Wl=(Wl, torch.bfloat16, W * W))
+                    G=(G, torch.bfloat16, ntile * 8192),
+                    Wl=(Wl, torch.bfloat16, 64 * 64))
     if mode == T.MBG_LAYER_LAST:
-        need.update(Q1=(Q1, torch.bfloat16, Hq * W), bq1=(bq1, torch.float32, Hq),
+        need.update(Q1=(Q1, torch.bfloat16, 128 * 64), bq1=(bq1, torch.float32, Hq),
                     q2=(q2, torch.float32, Hq), bq2=(bq2, torch.float32, 1),
                     y=(y, torch.float32, B * S))
     else:
-        need.update(v_out=(v_out, torch.bfloat16, B * S * W),
-                    F=(F, torch.bfloat16, 2 * Mo * S),
+        need.update(v_out=(v_out, torch.bfloat16, B * S * 64),
+                    F=(F, torch.bfloat16, ntile * 8192),
                     vhT=(vhT, torch.bfloat16, B * 2 * Mo * W))
     if bias is not None:
         need["bias"] = (bias, torch.float32, W)
@@ -174,6 +176,18 @@ def cast_bf16(x, y):
         raise ValueError("cast_bf16: sizes or dtype")
     _native.check(_lib().mbg_fno_cast_bf16(_ptr(x), _ptr(y), x.numel(),
                                            _stream()))
+
+
+def image_bf16(x, batch, rows, cols, ld, zs, R, K, img):
+    """img[z] = BF16 K-major core-matrix image of the R x K matrix with
+    entries x[z zs + r ld + c] (r < rows, c < cols; zero elsewhere)."""
+    if x.dtype != torch.float32 or img.dtype != torch.bfloat16:
+        raise ValueError("image_bf16: FP32 input, BF16 image")
+    _check_span(x, 0, [(batch, zs), (rows, ld), (cols, 1)], "image_bf16 x")
+    if img.numel() < batch * R * K or not img.is_contiguous():
+        raise ValueError("image_bf16: image too small")
+    _native.check(_lib().mbg_fno_image_bf16(_ptr(x), batch, rows, cols, ld,
+                                            zs, R, K, _ptr(img), _stream()))
 
 
 def colsum(x, rows, cols, row_stride, out):

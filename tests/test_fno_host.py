@@ -89,7 +89,7 @@ def test_inference_plan_equals_forward(monkeypatch, S_, fused):
     """FNO.infer computes the same network as forward(), through the CPU
     model of the kernels: as fused layer launches (S a multiple of 128:
     lifting + DFT, inverse DFT + pointwise + DFT, last layer + projection,
-    one mixing product per layer) and as products of the general kernel
+    two mixing products per layer) and as products of the general kernel
     (K-contiguous BF16 layouts, transposed activation copies, BF16 weight
     copies)."""
     from mbsolve_gb300 import surrogate as S

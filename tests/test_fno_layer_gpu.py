@@ -1,6 +1,7 @@
 """The fused Fourier-layer kernel (mbg_fno_spectral_layer) against the CPU
 model of its arithmetic (tests/fno_emulator.py: float64 sums of the same
-BF16-rounded operands, FP32 accumulators, BF16 stores), in all three modes:
+BF16-rounded operands, FP32 accumulators, BF16 stores; operands and
+activations as tile images), in all three modes, and the image kernel:
 at the surrogate's full width with more samples than SMs (each CTA walks
 several samples, tiles crossing sample boundaries in its pipeline) and at
 ragged sizes (W, Mo, Hq, Fi below the kernel's tile sizes, one sample per
@@ -34,16 +35,28 @@ def _rel(a, b):
 
 
 def _inputs(B, S, W, Mo, Fi, Hq, seed):
+    """Random operands in the kernel's layouts: activations, bases and dense
+    weights as BF16 tile images (channels, modes and rows beyond W, 2 Mo and
+    Hq zero)."""
     g = torch.Generator().manual_seed(seed)
-    b16 = torch.bfloat16
+    b16, T = torch.bfloat16, S // 128
     r = lambda *s: torch.randn(*s, generator=g)
+
+    def pad(x, R, K):
+        out = torch.zeros(x.shape[0], R, K)
+        out[:, :x.shape[1], :x.shape[2]] = x
+        return out
+
+    v = pad(r(B * T, 128, W), 128, 64)
+    G = pad(r(T, 128, 2 * Mo), 128, 64)
+    F = pad(r(T, 2 * Mo, 128) / S, 64, 128)
     return dict(
         X=r(B, S, Fi), P=r(W, Fi) / Fi ** 0.5,
-        v=r(B, S, W).to(b16), Y=r(B, 2, W, Mo).to(b16),
-        G=r(S, 2 * Mo).to(b16), Wl=(r(W, W) / W ** 0.5).to(b16),
-        bias=r(W) * 0.1, F=(r(2 * Mo, S) / S).to(b16),
-        Q1=(r(Hq, W) / W ** 0.5).to(b16), bq1=r(Hq) * 0.1,
-        q2=r(Hq) / Hq ** 0.5, bq2=r(1))
+        v=E.to_image(v).to(b16), Y=r(B, 2, Mo, W).to(b16),
+        G=E.to_image(G).to(b16), Wl=E.to_image(pad(r(1, W, W) / W ** 0.5, 64, 64)).to(b16),
+        bias=r(W) * 0.1, F=E.to_image(F).to(b16),
+        Q1=E.to_image(pad(r(1, Hq, W) / W ** 0.5, 128, 64)).to(b16),
+        bq1=r(Hq) * 0.1, q2=r(Hq) / Hq ** 0.5, bq2=r(1))
 
 
 @pytest.mark.parametrize("B,S,W,Mo,Fi,Hq", [(311, 256, 64, 32, 9, 128),
@@ -53,7 +66,7 @@ def test_layer_matches_model(K, mode, B, S, W, Mo, Fi, Hq):
     from mbsolve_gb300 import capi_types as T
     x = _inputs(B, S, W, Mo, Fi, Hq, seed=7 + mode)
     act = T.MBG_ACT_NONE if mode != T.MBG_LAYER_MID else T.MBG_ACT_GELU
-    outs = dict(v_out=torch.zeros(B * S * W, dtype=torch.bfloat16),
+    outs = dict(v_out=torch.zeros(B * S * 64, dtype=torch.bfloat16),
                 vhT=torch.zeros(B * 2 * Mo * W, dtype=torch.bfloat16),
                 y=torch.zeros(B * S))
     use = dict(x)
@@ -86,3 +99,18 @@ def test_layer_rejects_missing_operands(K):
     from mbsolve_gb300 import capi_types as T
     with pytest.raises(ValueError):
         K.spectral_layer(T.MBG_LAYER_MID, T.MBG_ACT_GELU, 2, 128, 64, 32)
+
+
+def test_image_kernel_matches_model(K):
+    g = torch.Generator().manual_seed(3)
+    x = torch.randn(3, 100, 50, generator=g)
+    for (batch, rows, cols, ld, zs, R, Kc) in [(3, 100, 50, 50, 5000, 104, 56),
+                                                (1, 40, 30, 50, 0, 64, 32),
+                                                (2, 50, 40, 50, 40, 64, 128)]:
+        n = batch * R * Kc
+        got = torch.zeros(n, dtype=torch.bfloat16, device="cuda")
+        K.image_bf16(x.cuda(), batch, rows, cols, ld, zs, R, Kc, got)
+        want = torch.zeros(n, dtype=torch.bfloat16)
+        E.image_bf16(x, batch, rows, cols, ld, zs, R, Kc, want)
+        torch.cuda.synchronize()
+        assert torch.equal(got.cpu(), want)
