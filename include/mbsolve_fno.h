@@ -124,7 +124,8 @@ enum {
  *             columns at i 8192 (rows 2 Mo..63 zero)
  *   Wl        pointwise weights [W][W]: their 64 x 64 image
  *   Q1        projection weights [Hq][W]: their 128 x 64 image
- * Plain layouts (row-major): X [B][S][Fi] FP32, P [W][Fi] FP32,
+ *   P         lifting weights [W][Fi]: their 64 x 16 image
+ * Plain layouts (row-major): X [B][S][Fi] FP32,
  * Y [B][2][Mo][W] BF16 (Re then Im of the mixed spectrum), bias [W] FP32
  * (NULL: zero), vhT [B][2 Mo][W] BF16, bq1, q2 [Hq], bq2 [1], y [B][S]
  * FP32. Every pointer 16-byte aligned.
@@ -143,7 +144,7 @@ typedef struct mbg_fno_layer_desc {
     int32_t act;      /* MBG_ACT_NONE or MBG_ACT_GELU */
     int32_t batch, S, W, Mo, Fi, Hq;
     const float* X;
-    const float* P;
+    const void* P;
     const void* v;
     const void* Y;
     const void* G;

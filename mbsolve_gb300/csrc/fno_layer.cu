@@ -7,7 +7,7 @@
 //
 //   first product   MID/LAST: acc = G Y^T + v Wl^T on the tensor cores
 //                   (two K = 64 operand pairs, tcgen05.mma, FP32 in TMEM);
-//                   LIFT: acc = X P^T on the CUDA cores (K = Fi <= 16)
+//                   LIFT: acc = X P^T (K = Fi <= 16, padded to 16)
 //   epilogue        u = acc + bias, GELU, rounded to BF16 once; stored as
 //                   the next activation v_out (MID, LIFT) and written into
 //                   shared memory as an MMA operand
@@ -21,8 +21,9 @@
 // Warp roles, coupled only by mbarriers (no block-wide barrier inside the
 // tile loop): warp 16 stages operands by bulk copies (TMA engine, one
 // instruction per 16 KB tile image) into rings of two (G, v) pairs (six X
-// tiles for the lifting) and four DFT-basis tiles, and transposes a
-// sample's mixed spectrum Y into its operand image; one thread of warp 17
+// tiles for the lifting, which the epilogue warps convert into BF16
+// operand images two tiles ahead) and four DFT-basis tiles, and transposes
+// a sample's mixed spectrum Y into its operand image; one thread of warp 17
 // issues the MMAs into two first-product and two
 // second-product TMEM accumulators; warps 0-15 run the epilogues (warp w
 // reads TMEM lanes 32 (w % 4) .. +31, columns 16 (w / 4) .. +15) and write
@@ -63,6 +64,9 @@ constexpr int B_IMG = 64 * 64 * 2;        // Y or Wl
 constexpr int IMG_ELEMS = IMG / 2;
 constexpr int NGV = 2, NX = 6, NFR = 4, NYR = 2;  // ring depths: (G, v) pairs, X tiles (LIFT), basis tiles, Y
 constexpr int X_SLOT = LT * 16 * 4;       // lifting input tile: 128 rows x <= 16 FP32 features
+constexpr int NXI = 3;                    // ring of lifting input images (BF16, 128 x 16)
+constexpr int XI_IMG = LT * 16 * 2;
+constexpr int OFF_XI = NX * X_SLOT;       // after the X tiles, in the first ring's space
 constexpr uint32_t VT_LBO = 144;          // transposed tile: K-direction core-matrix stride
 constexpr uint32_t VT_SBO = 16 * VT_LBO;  // 8-channel group stride
 constexpr int VT_IMG = 8 * VT_SBO;        // 64 channel rows x 128 samples
@@ -79,12 +83,12 @@ constexpr int OFF_OUT = OFF_VT + 2 * VT_IMG;  // output image (LIFT, MID)
 constexpr int OFF_Y = OFF_OUT + IMG;
 constexpr int OFF_W = OFF_Y + NYR * B_IMG;
 constexpr int OFF_SMALL = OFF_W + B_IMG;
-constexpr int SM_BIAS = 0, SM_BQ1 = 64, SM_Q2 = 192, SM_RED = 320, SM_P = 1344;  // floats
-constexpr int SMALL_FLOATS = SM_P + 16 * 64;
+constexpr int SM_BIAS = 0, SM_BQ1 = 64, SM_Q2 = 192, SM_RED = 320;  // floats
+constexpr int SMALL_FLOATS = SM_RED + 2 * 4 * 128;
 constexpr int LAYER_SMEM = OFF_SMALL + SMALL_FLOATS * 4 + 128;  // + alignment slack
 // the last basis slot's unread M rows (32 KB from its start) stay inside the map
 static_assert(OFF_F + (NFR - 1) * F_IMG + 2 * F_IMG <= OFF_OUT, "basis slot overrun");
-static_assert(NX * X_SLOT <= NGV * GV_SLOT && IMG <= NFR * F_IMG && IMG <= VT_IMG, "aliases");
+static_assert(NX * X_SLOT + NXI * XI_IMG <= NGV * GV_SLOT && IMG <= NFR * F_IMG && IMG <= VT_IMG, "aliases");
 static_assert(LAYER_SMEM + 512 <= 227 * 1024, "shared memory");
 
 constexpr uint32_t ID64 = idesc_bf16(128, 64);
@@ -102,13 +106,14 @@ enum {
     B_FOP = 28, B_EOP = 30,  // epilogue-written MMA operand: epilogue warps / second-product MMA
     B_FD = 32, B_ED = 34,    // DFT accumulators: a sample's last DFT MMA / epilogue warps
     B_FH = 36, B_EH = 38,    // projection accumulators: MMA / epilogue warps
-    NBAR = 40
+    B_FXI = 40, B_EXI = 43,  // lifting input images: copy warp / lifting MMA
+    NBAR = 46
 };
 
 struct layer_params {
     int32_t mode, act, batch, S, W, Mo, Fi, Hq;
     const float* X;
-    const float* P;
+    const __nv_bfloat16* P;
     const __nv_bfloat16* v;
     const __nv_bfloat16* Y;
     const __nv_bfloat16* G;
@@ -196,7 +201,8 @@ __global__ void __launch_bounds__(LNTH, 1) spectral_layer_kernel(const layer_par
         for (int k = 0; k < NBAR; k++) {
             uint32_t cnt = 1;
             if (k == B_EACC || k == B_EACC + 1 || k == B_FOP || k == B_FOP + 1 || k == B_ED || k == B_ED + 1 ||
-                k == B_EH || k == B_EH + 1 || (lift && k >= B_EGV && k < B_EGV + NX))
+                k == B_EH || k == B_EH + 1 || (k >= B_FXI && k < B_FXI + NXI) ||
+                (lift && k >= B_EGV && k < B_EGV + NX))
                 cnt = NEPI / 32;  // one arrival per epilogue warp
             mbar_init(bar(k), cnt);
         }
@@ -204,8 +210,7 @@ __global__ void __launch_bounds__(LNTH, 1) spectral_layer_kernel(const layer_par
         abort_sh = 0;
     }
     // per-CTA constants: bias, projection vectors (q2 in BF16, as a product
-    // operand), lifting weights (BF16-rounded, [feature][channel]); the
-    // dense weights' images
+    // operand); the dense weights' images
     for (int c = tid; c < 64; c += LNTH) small[SM_BIAS + c] = (p.bias && c < p.W) ? p.bias[c] : 0.0f;
     if (last) {
         for (int j = tid; j < 128; j += LNTH) {
@@ -214,10 +219,7 @@ __global__ void __launch_bounds__(LNTH, 1) spectral_layer_kernel(const layer_par
         }
     }
     if (lift) {
-        for (int e = tid; e < 16 * 64; e += LNTH) {
-            const int f = e >> 6, c = e & 63;
-            small[SM_P + e] = (f < p.Fi && c < p.W) ? bf16r(p.P[c * p.Fi + f]) : 0.0f;
-        }
+        for (int e = tid; e < 64 * 16 * 2 / 16; e += LNTH) cp_async16(sb + OFF_W + e * 16, p.P + e * 8, 16u);
     } else {
         for (int e = tid; e < B_IMG / 16; e += LNTH) cp_async16(sb + OFF_W + e * 16, p.Wl + e * 8, 16u);
     }
@@ -322,7 +324,6 @@ __global__ void __launch_bounds__(LNTH, 1) spectral_layer_kernel(const layer_par
                 idle = did ? 0 : idle + 1;
                 if (idle >= WAIT_LIMIT) *abort = 1;
                 stop = *abort;
-                if (!did) __nanosleep(32);
             }
             if (__shfl_sync(0xFFFFFFFFu, stop, 0)) break;
         }
@@ -333,11 +334,25 @@ __global__ void __launch_bounds__(LNTH, 1) spectral_layer_kernel(const layer_par
         // tile ud's first).
         if (lane == 0) {
             const int nk1 = (2 * p.Mo + 15) / 16, nk2 = (p.W + 15) / 16;
-            int ui = lift ? n : 0, ud = 0;
+            int ui = 0, ud = 0;
             uint32_t idle = 0;
             while (ud < n) {
                 bool did = false;
-                if (ui < n) {
+                if (lift && ui < n) {
+                    // lifting: acc = X_image P_image^T (K = 16)
+                    const int xi = ui % NXI;
+                    if (mbar_peek(bar(B_FXI + xi), (ui / NXI) & 1) &&
+                        mbar_peek(bar(B_EACC + (ui & 1)), ((ui >> 1) & 1) ^ 1)) {
+                        fence_after();
+                        mma_bf16(tmem + (uint32_t) ((ui & 1) * 64),
+                                 smem_desc_nsw(sb + OFF_GV + OFF_XI + (uint32_t) (xi * XI_IMG), 128, 256),
+                                 smem_desc_nsw(sb + OFF_W, 128, 256), ID64, 0u);
+                        mma_commit(bar(B_FACC + (ui & 1)));
+                        mma_commit(bar(B_EXI + xi));
+                        ui++;
+                        did = true;
+                    }
+                } else if (ui < n) {
                     const int s = ui / T, i = ui % T, g = ui % NG;
                     if (mbar_peek(bar(B_FGV + g), (ui / NG) & 1) &&
                         (i != 0 || mbar_peek(bar(B_FY + s % NYR), (s / NYR) & 1)) &&
@@ -399,7 +414,6 @@ __global__ void __launch_bounds__(LNTH, 1) spectral_layer_kernel(const layer_par
                 idle = did ? 0 : idle + 1;
                 if (idle >= WAIT_LIMIT) *abort = 1;
                 if (*abort) break;
-                if (!did) __nanosleep(32);
             }
         }
     } else {
@@ -457,30 +471,38 @@ __global__ void __launch_bounds__(LNTH, 1) spectral_layer_kernel(const layer_par
                     ((red[lrow] + red[128 + lrow]) + (red[256 + lrow] + red[384 + lrow])) + p.bq2[0];
         };
 
+        // (LIFT) X tile uc (FP32 [128][Fi]) -> its BF16 input image 128 x 16
+        // (features >= Fi zero); each thread four features of one row
+        auto convert = [&](int uc) {
+            const int x = uc % NX, xi = uc % NXI;
+            wait_bar_warp(bar(B_FGV + x), (uc / NX) & 1, abort, lane);
+            wait_bar_warp(bar(B_EXI + xi), ((uc / NXI) & 1) ^ 1, abort, lane);
+            const int r = tid >> 2, k0 = (tid & 3) * 4;
+            const float* xs = reinterpret_cast<const float*>(sbp + OFF_GV + x * X_SLOT) + r * p.Fi;
+            float f4[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) f4[k] = (k0 + k < p.Fi) ? xs[k0 + k] : 0.0f;
+            const uint32_t a = sb + OFF_GV + OFF_XI + (uint32_t) (xi * XI_IMG) + koff(r, k0 >> 3, 2) +
+                (uint32_t) ((k0 & 7) * 2);
+            asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(a), "r"(pack_bf16(f4[0], f4[1])),
+                         "r"(pack_bf16(f4[2], f4[3]))
+                         : "memory");
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(bar(B_FXI + xi));
+                mbar_arrive(bar(B_EGV + x));
+            }
+        };
+        if (lift) {
+            if (n > 0) convert(0);
+            if (n > 1) convert(1);
+        }
+
+        int s = 0, i = 0;  // sample and tile of tile u
         for (int u = 0; u < n; u++) {
-            const int s = u / T, i = u % T;
             float x[16];
-            if (lift) {
-                const int g = u % NX;
-                wait_bar_warp(bar(B_FGV + g), (u / NX) & 1, abort, lane);
-                const float* xs = reinterpret_cast<const float*>(sbp + OFF_GV + g * X_SLOT) + lrow * p.Fi;
-#pragma unroll
-                for (int j = 0; j < 16; j++) x[j] = 0.0f;
-                for (int f = 0; f < p.Fi; f++) {
-                    const float xv = bf16r(xs[f]);
-                    const float4* w4 = reinterpret_cast<const float4*>(small + SM_P + f * 64 + qt * 16);
-#pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        const float4 wq = w4[q];
-                        x[4 * q] = fmaf(xv, wq.x, x[4 * q]);
-                        x[4 * q + 1] = fmaf(xv, wq.y, x[4 * q + 1]);
-                        x[4 * q + 2] = fmaf(xv, wq.z, x[4 * q + 2]);
-                        x[4 * q + 3] = fmaf(xv, wq.w, x[4 * q + 3]);
-                    }
-                }
-                __syncwarp();
-                if (lane == 0) mbar_arrive(bar(B_EGV + g));
-            } else {
+            {
                 wait_bar_warp(bar(B_FACC + (u & 1)), (u >> 1) & 1, abort, lane);
                 fence_after();
                 tmem_ld16(tmem + tlane + (uint32_t) ((u & 1) * 64 + qt * 16), x);
@@ -540,6 +562,11 @@ __global__ void __launch_bounds__(LNTH, 1) spectral_layer_kernel(const layer_par
                 if (lane == 0) mbar_arrive(bar(B_FOP + (u & 1)));
                 if (u >= 1) project(u - 1);
             }
+            if (lift && u + 2 < n) convert(u + 2);
+            if (++i == T) {
+                i = 0;
+                s++;
+            }
         }
         if (n > 0) {
             if (!last) readout(nsamp - 1);
@@ -595,7 +622,7 @@ void spectral_layer(const mbg_fno_layer_desc* d, cudaStream_t s)
     p.Fi = d->Fi;
     p.Hq = d->Hq;
     p.X = d->X;
-    p.P = d->P;
+    p.P = static_cast<const __nv_bfloat16*>(d->P);
     p.v = static_cast<const __nv_bfloat16*>(d->v);
     p.Y = static_cast<const __nv_bfloat16*>(d->Y);
     p.G = static_cast<const __nv_bfloat16*>(d->G);

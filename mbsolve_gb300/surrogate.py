@@ -272,7 +272,9 @@ class FNO:
             K.image_bf16(self.p[name], 1, W, W, W, 0, 64, 64, im[name])
         if "Q1" not in im:
             im["Q1"] = torch.empty(128 * 64, dtype=b16, device=d)
+            im["P"] = torch.empty(64 * 16, dtype=b16, device=d)
         K.image_bf16(self.p["Q1"], 1, Hq, W, W, 0, 128, 64, im["Q1"])
+        K.image_bf16(self.p["P"], 1, W, sh.F, sh.F, 0, 64, 16, im["P"])
 
     def _fbuffers(self, B):
         key = ("fused", B)
@@ -318,7 +320,7 @@ class FNO:
         im = self._img
         vhT, Y = b["VhT"], b["Y"]
         K.spectral_layer(T.MBG_LAYER_LIFT, T.MBG_ACT_NONE, B, S, W, Mo, Fi=Fi,
-                         X=X, P=p["P"], bias=p["bp"], v_out=b["v"][0],
+                         X=X, P=im["P"], bias=p["bp"], v_out=b["v"][0],
                          F=im["F"], vhT=vhT)
         cur = 0
         for l in range(L):

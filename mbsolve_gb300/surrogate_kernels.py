@@ -122,7 +122,7 @@ def spectral_layer(mode, act, batch, S, W, Mo, Fi=0, Hq=0, X=None, P=None,
                    F=None, vhT=None, Q1=None, bq1=None, q2=None, bq2=None,
                    y=None):
     """One Fourier layer of inference in one launch (mbg_fno_spectral_layer):
-    mode MBG_LAYER_LIFT (X [B, S, Fi], P [W, Fi] FP32), MBG_LAYER_MID (v
+    mode MBG_LAYER_LIFT (X [B, S, Fi] FP32, P image [64 16] BF16), MBG_LAYER_MID (v
     activation images [B S 64], Y [B, 2, Mo, W], G images [S/128, 8192],
     Wl image [64 64], BF16) or MBG_LAYER_LAST (the same plus the Q1 image
     [128 64] BF16, bq1, q2 [Hq], bq2 [1] FP32 and y [B, S] FP32); LIFT and
@@ -132,7 +132,7 @@ def spectral_layer(mode, act, batch, S, W, Mo, Fi=0, Hq=0, X=None, P=None,
     B, ntile = int(batch), int(S) // 128
     need = {}
     if mode == T.MBG_LAYER_LIFT:
-        need.update(X=(X, torch.float32, B * S * Fi), P=(P, torch.float32, W * Fi))
+        need.update(X=(X, torch.float32, B * S * Fi), P=(P, torch.bfloat16, 64 * 16))
     else:
         need.update(v=(v, torch.bfloat16, B * S * 64),
                     Y=(Y, torch.bfloat16, B * 2 * W * Mo),

@@ -92,7 +92,8 @@ def spectral_layer(mode, act, batch, S, W, Mo, Fi=0, Hq=0, X=None, P=None,
     B, M2, T = batch, 2 * Mo, S // 128
     f32, f64, b16 = torch.float32, torch.float64, torch.bfloat16
     if mode == 0:
-        u = _bf(_flat(X, B * S * Fi, (B, S, Fi))) @ _bf(_flat(P, W * Fi, (W, Fi))).T
+        Pm = _bf(from_image(P, 1, 64, 16)[0, :W, :Fi])
+        u = _bf(_flat(X, B * S * Fi, (B, S, Fi))) @ Pm.T
     else:
         Yv = _bf(_flat(Y, B * 2 * Mo * W, (B, 2, Mo, W)))
         Yf = Yv.permute(0, 3, 1, 2).reshape(B, W, M2)          # [B, W, 2 Mo]

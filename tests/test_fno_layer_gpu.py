@@ -51,7 +51,7 @@ def _inputs(B, S, W, Mo, Fi, Hq, seed):
     G = pad(r(T, 128, 2 * Mo), 128, 64)
     F = pad(r(T, 2 * Mo, 128) / S, 64, 128)
     return dict(
-        X=r(B, S, Fi), P=r(W, Fi) / Fi ** 0.5,
+        X=r(B, S, Fi), P=E.to_image(pad(r(1, W, Fi) / Fi ** 0.5, 64, 16)).to(b16),
         v=E.to_image(v).to(b16), Y=r(B, 2, Mo, W).to(b16),
         G=E.to_image(G).to(b16), Wl=E.to_image(pad(r(1, W, W) / W ** 0.5, 64, 64)).to(b16),
         bias=r(W) * 0.1, F=E.to_image(F).to(b16),
