@@ -294,7 +294,8 @@ def cpu_child(args, timeout=900):
                        cwd=ROOT, env=env, capture_output=True, text=True,
                        timeout=timeout)
     if r.returncode != 0:
-        raise RuntimeError("cpu baseline failed: %s" % r.stderr[-2000:])
+        raise RuntimeError("cpu baseline failed (exit %d): %s %s" % (
+            r.returncode, r.stderr[-2000:], r.stdout[-1000:]))
     for line in reversed(r.stdout.splitlines()):
         if line.startswith("{"):
             return json.loads(line)

@@ -12,8 +12,10 @@ baseline, with the flags of the reference's own solver-cpu build
 default FP contraction) into oracle/_build/libmb_baseline.so. The
 reference's -march=native is replaced by the host CPU's named target
 (Arm: -mcpu of the Neoverse core the machine reports, e.g. neoverse-v2 on
-Grace; x86: -march=x86-64-v3), so that the build does not depend on the
-machine beyond its CPU model. Only timed, never used as the checker.
+Grace, with +nosve where the kernel does not report SVE; x86:
+-march=x86-64-v3), kept only if a small vectorised probe built with it
+runs on the host, so that the build does not depend on the machine beyond
+its CPU model. Only timed, never used as the checker.
 """
 import os
 import subprocess
@@ -75,30 +77,63 @@ def _cxx_accepts(flag):
     return r.returncode == 0
 
 
+def _cxx_runs(flags):
+    """A vectorised, OpenMP-SIMD loop built with `flags` runs on this host:
+    a CPU model's target can use extensions (SVE on Arm) that the running
+    kernel does not enable."""
+    import tempfile
+    src = ("#include <cstdio>\nint main() { float a[512], b[512], s = 0.f;\n"
+           "for (int i = 0; i < 512; i++) { a[i] = i * 0.5f; b[i] = 2.f - i; }\n"
+           "#pragma omp simd reduction(+ : s)\n"
+           "for (int i = 0; i < 512; i++) s += a[i] * b[i] + a[i] / (1.f + b[i] * b[i]);\n"
+           "std::printf(\"%g\\n\", s); return 0; }\n")
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "probe")
+        r = subprocess.run([os.environ.get("CXX", "g++"), "-O3", "-fopenmp"] +
+                           flags + ["-x", "c++", "-", "-o", exe], input=src,
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            return False
+        try:
+            return subprocess.run([exe], capture_output=True,
+                                  timeout=20).returncode == 0
+        except (OSError, subprocess.TimeoutExpired):
+            return False
+
+
+def _cpuinfo(key):
+    """The first value of `key` in /proc/cpuinfo (lower case), or None."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(key):
+                    return line.split(":", 1)[1].strip().lower()
+    except OSError:
+        pass
+    return None
+
+
 def cpu_target_flags():
-    """The named target for this host CPU (see the module docstring)."""
+    """The named target for this host CPU (see the module docstring), with
+    SVE switched off where the kernel does not report it (virtual machines
+    may hide it), and kept only if a probe built with it runs here."""
     import platform
     m = platform.machine()
     if m in ("aarch64", "arm64"):
-        part = None
-        try:
-            with open("/proc/cpuinfo") as f:
-                for line in f:
-                    if line.lower().startswith("cpu part"):
-                        part = line.split(":")[1].strip().lower()
-                        break
-        except OSError:
-            pass
+        part = _cpuinfo("cpu part")
         # Arm Ltd. part numbers of the Neoverse cores
         names = {"0xd4f": "neoverse-v2", "0xd40": "neoverse-v1",
                  "0xd0c": "neoverse-n1", "0xd49": "neoverse-n2",
                  "0xd84": "neoverse-v3"}
         flag = "-mcpu=" + names.get(part, "neoverse-v2")
-        return [flag] if _cxx_accepts(flag) else []
-    if m in ("x86_64", "AMD64"):
-        return ["-march=x86-64-v3"] if _cxx_accepts("-march=x86-64-v3") \
-            else []
-    return []
+        feats = (_cpuinfo("features") or "").split()
+        if "sve" not in feats and "n1" not in flag:
+            flag += "+nosve"
+    elif m in ("x86_64", "AMD64"):
+        flag = "-march=x86-64-v3"
+    else:
+        return []
+    return [flag] if _cxx_accepts(flag) and _cxx_runs([flag]) else []
 
 
 def baseline_flags():

@@ -46,11 +46,16 @@ def cpu_info():
                 k, v = line.split(":", 1)
                 kv[k.strip()] = v.strip()
         info["model"] = kv.get("Model name") or kv.get("Vendor ID")
-        cores = int(kv.get("Core(s) per socket", "0") or 0) * \
-            int(kv.get("Socket(s)", "1") or 1)
+
+        def num(key, default):
+            v = kv.get(key, "")
+            return int(v) if v.isdigit() else default
+        # Arm hosts report cores per cluster and "-" sockets
+        per = num("Core(s) per socket", 0) or num("Core(s) per cluster", 0)
+        cores = per * (num("Socket(s)", 0) or num("Cluster(s)", 1))
         if cores:
             info["physical_cores"] = cores
-        info["threads_per_core"] = int(kv.get("Thread(s) per core", "1") or 1)
+        info["threads_per_core"] = num("Thread(s) per core", 1)
     except Exception as e:  # lscpu missing: /proc/cpuinfo
         info["lscpu"] = "unavailable: %s" % e
     try:
