@@ -58,7 +58,8 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t ad, uint64_t bd
         "setp.ne.b32 p, %4, 0;\n"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
         "}\n" ::"r"(tmem),
-        "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+        : "memory");
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t mbar)

@@ -19,12 +19,15 @@
 // are never updated; the reference's index rules (no H update at i = 0,
 // H[N] = 0) give them no influence on the run.
 //
-// FP32 kernels keep E and H as unevaluated sums hi + lo of two floats and
-// update them with error-free transformations (TwoSum; TwoProd by fma):
-// the spatial differences of FP32 fields lose about log2(points per
-// wavelength) bits, which over 1e5 steps dominates the error; with the
-// double-float fields the FP32 result tracks the FP64 one closely while
-// density, polarisation and all matrix work stay in FP32.
+// FP32 kernels keep the density state, and E and H in all but the 2-level
+// kernel, as unevaluated sums hi + lo of two floats updated with
+// error-free transformations (TwoSum; TwoProd by fma): the spatial
+// differences of FP32 fields lose about log2(points per wavelength) bits,
+// and the per-step rounding of small density increments accumulates; with
+// the float pairs the FP32 result tracks the FP64 one to ~1e-7 while
+// polarisation and all matrix work stay in FP32. The 2-level kernel keeps
+// E and H in plain FP32 (one rounding per update by fma): ~6e-6 over 1e5
+// steps, within the 1e-5 target, for 22 % more throughput.
 #pragma once
 
 #include <cuda_runtime.h>

@@ -59,7 +59,14 @@ __device__ __forceinline__ bool tile_steps(
     T* sh_bl,
     tc::ctx* tcc = nullptr)
 {
-    constexpr bool DF = sizeof(T) == 4;
+    // FP32: the density state is a float pair (hi + lo) throughout; E and H
+    // are float pairs except in the 2-level coherence-vector kernel, where
+    // plain FP32 fields (one rounding per update, coefficients in
+    // registers) hold the probe error near 6e-6 at 100,000 steps, under
+    // the 1e-5 target, at 22 % more cell-updates/s (measured variant by
+    // variant: a plain FP32 coherence vector instead broke 1e-5)
+    constexpr bool DFD = sizeof(T) == 4;
+    constexpr bool DF = DFD && !(ALGO == 1 && LEV == 2);
     constexpr int D = density_len<ALGO, LEV>::value;
     constexpr int NW = NT / 32;
     constexpr bool TCU = TC && UNIFORM;  // density products on the tensor cores
@@ -76,7 +83,7 @@ __device__ __forceinline__ bool tile_steps(
         return UNIFORM ? sh_coef : p.mc + (uint64_t) (M[j] >= 0 ? M[j] : 0) * p.mstride;
     };
     fcoef fu;
-    if constexpr (DF && UNIFORM) fu = load_fcoef(sh_coef);
+    if constexpr (DFD && UNIFORM) fu = load_fcoef(sh_coef);
     const bool qm_uniform = UNIFORM && sh_coef[pre::FD_HAS_QM] != T(0);
     using creg_t = typename std::conditional<REGCOEF, cvr_coef_reg<T, 3>, no_coef>::type;
     const creg_t creg(sh_coef);
@@ -132,6 +139,9 @@ __device__ __forceinline__ bool tile_steps(
                 const T hnl = (j + 1 < C) ? Hl[j + 1] : hrl;
                 const fcoef f = UNIFORM ? fu : load_fcoef(block(j));
                 df_e_update(E[j], El[j], hn - H[j], hnl - Hl[j], P[j], f);
+            } else if constexpr (DFD) {
+                const fcoef f = UNIFORM ? fu : load_fcoef(block(j));
+                E[j] = fmaf(f.a, E[j], fmaf(f.bh, hn - H[j], -f.g * P[j]));
             } else {
                 const T* cb = block(j);
                 E[j] = cb[pre::FD_A] * E[j] +
@@ -180,6 +190,9 @@ __device__ __forceinline__ bool tile_steps(
                     const T epl = (j > 0) ? El[j - 1] : ell;
                     const fcoef f = UNIFORM ? fu : load_fcoef(block(j));
                     df_h_update(H[j], Hl[j], E[j] - ep, El[j] - epl, f);
+                } else if constexpr (DFD) {
+                    const fcoef f = UNIFORM ? fu : load_fcoef(block(j));
+                    H[j] = fmaf(f.ch, E[j] - ep, H[j]);
                 } else {
                     H[j] += block(j)[pre::FD_C] * (E[j] - ep);
                 }
@@ -237,7 +250,7 @@ __device__ __forceinline__ bool tile_steps(
                 const T e = DF ? E[j] + El[j] : E[j];
                 if constexpr (ALGO == 1) {
                     if constexpr (REGCOEF) {
-                        if constexpr (DF)
+                        if constexpr (DFD)
                             cvr_update_df<D>(R[j], Rl[j], e, P[j], creg);
                         else
                             cvr_update<T, D>(R[j], e, P[j], creg);
@@ -248,18 +261,18 @@ __device__ __forceinline__ bool tile_steps(
                         tc::cvr_update_df_row<D>(tcc->rows + threadIdx.x * D, R[j], Rl[j], e, P[j], cf);
                     } else if constexpr (PADC) {
                         const cvr_coef_pad<T, D> cf{ (uint32_t) __cvta_generic_to_shared(sh_coef), sh_coef };
-                        if constexpr (DF)
+                        if constexpr (DFD)
                             cvr_update_df<D>(R[j], Rl[j], e, P[j], cf);
                         else
                             cvr_update<T, D>(R[j], e, P[j], cf);
                     } else {
                         cvr_coef<T, D> cf{ cb };
-                        if constexpr (DF)
+                        if constexpr (DFD)
                             cvr_update_df<D>(R[j], Rl[j], e, P[j], cf);
                         else
                             cvr_update<T, D>(R[j], e, P[j], cf);
                     }
-                } else if constexpr (DF) {
+                } else if constexpr (DFD) {
                     cayley_update_df<LEV>(R[j], Rl[j], e, P[j], cb);
                 } else {
                     cayley_update<T, LEV>(R[j], e, P[j], cb);
@@ -289,7 +302,7 @@ __device__ __forceinline__ bool tile_steps(
                         case 0: v = ev; break;
                         case 1: v = P[j]; break;
                         case 2: v = hv; break;
-                        case 4: v = DF ? (R[j][1] - R[j][0]) + (Rl[j][1] - Rl[j][0]) : R[j][1] - R[j][0]; break;
+                        case 4: v = DFD ? (R[j][1] - R[j][0]) + (Rl[j][1] - Rl[j][0]) : R[j][1] - R[j][0]; break;
                         default: {
                             // populations (3) and coherence parts (REC_COH_*):
                             // an entry of the packed matrix (diagonal, then
@@ -302,7 +315,7 @@ __device__ __forceinline__ bool tile_steps(
                                                             (rc.type == REC_COH_IM ? 1 : 0);
 #pragma unroll
                             for (int q = 0; q < LEV * LEV; q++)
-                                if (idx == (uint32_t) q) v = DF ? R[j][q] + Rl[j][q] : R[j][q];
+                                if (idx == (uint32_t) q) v = DFD ? R[j][q] + Rl[j][q] : R[j][q];
                             if (rc.type == REC_COH_IM && rc.row_idx > rc.col_idx) v = -v;
                             break;
                         }
@@ -311,7 +324,7 @@ __device__ __forceinline__ bool tile_steps(
                         constexpr int DDv = D > 0 ? D : 1;
                         T u[DDv];
 #pragma unroll
-                        for (int q = 0; q < DDv; q++) u[q] = DF ? R[j][q] + Rl[j][q] : R[j][q];
+                        for (int q = 0; q < DDv; q++) u[q] = DFD ? R[j][q] + Rl[j][q] : R[j][q];
                         // the padded shared copy lacks the record rows, the
                         // staged copy the coherence rows
                         const T* rb = (PADC || rc.type >= REC_COH_RE) ? p.mc + (uint64_t) M[j] * p.mstride

@@ -14,9 +14,9 @@ from tests import helpers
 pytestmark = pytest.mark.gpu
 
 # relative L2 error per record against the reference's FP64 result. FP32
-# keeps E, H and the density state (coherence vector or Cayley density
-# matrix) as float pairs, with the field-free part of every step from the
-# FP64 precompute.
+# keeps the density state (coherence vector or Cayley density matrix), and
+# E and H in all but the 2-level kernel, as float pairs, with the
+# field-free part of every step from the FP64 precompute.
 TOL = {"fp64": 1e-9, "fp32": 1e-5}
 
 
