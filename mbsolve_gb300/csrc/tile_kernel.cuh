@@ -11,6 +11,7 @@
 #include "kernels.cuh"
 #include "tc_density.cuh"
 #include "bulk_stage.cuh"
+#include "pair_steps.cuh"
 
 namespace mbg {
 
@@ -575,10 +576,15 @@ __device__ __forceinline__ void step_body(const kparams<T>& p, uint32_t tile, ui
     }
 
     if (uniform) {
-        const bool ok = tile_steps<T, ALGO, LEV, C, NT, true, TC>(p, td, rd, l0, nsteps, step0, E, El, H, Hl, P,
-                                                                  R, Rl, M, sh_coef, tl, sh_a, sh_al, sh_b,
-                                                                  sh_bl, &tcc);
-        if (!ok && threadIdx.x == 0) atomicOr(p.status, STATUS_TC_WAIT);
+        if constexpr (pair_path<T, ALGO, LEV, C, TC>()) {
+            // two points per instruction (pair_steps.cuh)
+            tile_steps_pair<C, NT>(p, td, rd, l0, nsteps, step0, E, H, P, R, Rl, M, sh_coef, tl, sh_a, sh_b);
+        } else {
+            const bool ok = tile_steps<T, ALGO, LEV, C, NT, true, TC>(p, td, rd, l0, nsteps, step0, E, El, H, Hl,
+                                                                      P, R, Rl, M, sh_coef, tl, sh_a, sh_al,
+                                                                      sh_b, sh_bl, &tcc);
+            if (!ok && threadIdx.x == 0) atomicOr(p.status, STATUS_TC_WAIT);
+        }
     } else {
         tile_steps<T, ALGO, LEV, C, NT, false>(p, td, rd, l0, nsteps, step0, E, El, H, Hl, P, R, Rl, M,
                                                sh_coef, tl, sh_a, sh_al, sh_b, sh_bl);

@@ -83,6 +83,68 @@ def test_tuning_does_not_change_results(native, name, setup, kw):
             assert np.array_equal(a, b)
 
 
+def _sit_split(n, steps, split):
+    """The self-induced-transparency medium of setups.sit_2lvl over n points
+    with whole-grid records of E, H, P and the inversion every 25 steps;
+    split > 0 cuts it into regions of `split` points that alternate between
+    two materials with the same parameters, so that every tile holds two
+    materials."""
+    L = setups.LENGTH_2LVL * (n - 1) / 16383.0
+    qm = mb.qm_desc_2lvl(1e24, 2 * mb.PI * 2e14, setups.DIPOLE / mb.E0,
+                         1e9, 1e12, -1.0)
+    mats = [mb.material("split_%s_%d_%d" % (k, n, split), qm) for k in "ab"]
+    for m in mats:
+        mb.material.add_to_library(m)
+    dev = mb.device("split")
+    if split <= 0:
+        dev.add_region(mb.region("all", mats[0], 0.0, L))
+    else:
+        dx = L / (n - 1)
+        for k, x0 in enumerate(range(0, n, split)):
+            x1 = min(x0 + split, n - 1)
+            dev.add_region(mb.region("r%d" % k, mats[k % 2], x0 * dx,
+                                     x1 * dx))
+    sce = mb.scenario("split", n, setups._courant_endtime(n, L, steps),
+                      mb.ic_density_const(mb.qm_operator([1, 0])),
+                      mb.ic_field_const(0.0), mb.ic_field_const(0.0))
+    sce.add_source(mb.sech_pulse("sech", 0.0, mb.source.hard_source,
+                                 setups.sech_area_amplitude(2.5), 2e14,
+                                 15.0, setups.BETA))
+    dt = sce.get_endtime() / (steps - 1.5)
+    for name in ("e", "h", "p", "inv12"):
+        sce.add_record(mb.record(name, 25 * dt))
+    sce.add_record(mb.record("e_probe", 0.0, L))
+    return dev, sce
+
+
+def test_pair_path_equals_scalar_path(native):
+    """The 2-level FP32 kernel updates uniform tiles two points per
+    instruction (packed FP32 pairs) and tiles of several materials one
+    point at a time, each with the same roundings: the same medium as one
+    material and as alternating copies of it gives equal results at every
+    point, at every shape (C = 1 keeps the one-point loop on uniform tiles
+    too)."""
+    n, steps = 2900, 600
+    ref = None
+    for split in (37, 0):
+        for c_, nt, d in ([(4, 128, 16)] if split else
+                          [(1, 128, 8), (2, 128, 8), (4, 128, 16),
+                           (4, 256, 32), (8, 128, 7)]):
+            mb.material.clear_library()
+            dev, sce = _sit_split(n, steps, split)
+            _, res = helpers.gpu_results("gpu-fdtd-2lvl-cvr-rodr-fp32", dev,
+                                         sce, helpers.tuning(c_, nt, d, 2))
+            assert all(np.isfinite(r).all() for r in res)
+            if ref is None:
+                ref = res
+                # the pulse has crossed part of the medium
+                assert np.abs(ref[0]).max() > 0.0
+                continue
+            for k, (a, b) in enumerate(zip(res, ref)):
+                assert np.array_equal(a, b), (split, c_, nt, d, k,
+                                              np.abs(a - b).max())
+
+
 def test_run_twice_continues_like_reference(native):
     from oracle import oracle as O
     dev, sce = setups.ziolkowski1995(1024, 30e-15)
