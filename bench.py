@@ -523,7 +523,8 @@ def run_ours(args, dist):
                 "blocking keeps the state on chip for depth steps, so "
                 "achieved may exceed the copy peak while DRAM (dram_frac) "
                 "and the kernel's own state (state_frac) stay far below it: "
-                "the kernel is bound by instruction issue"})
+                "the kernel is bound by its arithmetic (FMA pipe and "
+                "instruction issue: fma_pipe_active, issue_active)"})
 
     line = {
         "metric": METRIC, "value": value, "unit": "cell-updates/s",
