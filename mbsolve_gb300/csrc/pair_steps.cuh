@@ -75,11 +75,25 @@ struct cvr2_pair_coef {
     }
 };
 
+// The couplings that the plane basis of a 2-level medium with a diagonal
+// Hamiltonian and a real dipole leaves exactly zero: the field rotates the
+// (0, 1) plane, the free evolution couples 0 and 2 (precession) and relaxes
+// 1 on its own, and P reads 0 and 2. A uniform tile whose block has them
+// zero skips their products (a product with an exact zero changes no sum).
+__device__ __forceinline__ bool cvr2_sparse(const float* cb)
+{
+    const cvr_coef<float, 3> c{ cb };
+    return c.Bd(0, 1) == 0.0f && c.Bd(1, 0) == 0.0f && c.Bd(1, 2) == 0.0f && c.Bd(2, 1) == 0.0f &&
+        c.Bdl(0, 1) == 0.0f && c.Bdl(1, 0) == 0.0f && c.Bdl(1, 2) == 0.0f && c.Bdl(2, 1) == 0.0f &&
+        c.g(1) == 0.0f;
+}
+
 // cvr_update_df<3> on two points: the rotation of the (0, 1) plane by
 // theta dt e (rot_coeffs' series, its negated Horner chain for 1 - cos
 // giving the same roundings), the correction k + Bd r with its low-word
 // part Bdl r, the error-free accumulation and renormalisation of the pair
-// words, and P = p0 + g . v.
+// words, and P = p0 + g . v. SP: the zeros of cvr2_sparse are skipped.
+template<bool SP>
 __device__ __forceinline__ void cvr2_update_pair(float2 (&uh)[3], float2 (&ul)[3], float2 e, float2& pout,
                                                  const cvr2_pair_coef& c)
 {
@@ -111,6 +125,7 @@ __device__ __forceinline__ void cvr2_update_pair(float2 (&uh)[3], float2 (&ul)[3
         sl[i] = z;
 #pragma unroll
         for (int j = 0; j < 3; j++) {
+            if (SP && (i == 1) != (j == 1)) continue;
             s[i] = fma(c.bd[i * 3 + j], r[j], s[i]);
             sl[i] = fma(c.bdl[i * 3 + j], r[j], sl[i]);
         }
@@ -132,7 +147,7 @@ __device__ __forceinline__ void cvr2_update_pair(float2 (&uh)[3], float2 (&ul)[3
         h = t;
         uh[i] = h;
         ul[i] = l;
-        pp = fma(c.g[i], h, fma(c.g[i], l, pp));
+        if (!SP || i != 1) pp = fma(c.g[i], h, fma(c.g[i], l, pp));
     }
     pout = pp;
 }
@@ -151,8 +166,9 @@ struct pair_view {
     }
 };
 
-// TL: tile_lists (tile_kernel.cuh)
-template<int C, int NT, class TL>
+// TL: tile_lists (tile_kernel.cuh); SP: the tile's block has the zeros of
+// cvr2_sparse
+template<int C, int NT, bool SP, class TL>
 __device__ __forceinline__ void tile_steps_pair(
     const kparams<float>& p,
     const tile_desc& td,
@@ -244,7 +260,7 @@ __device__ __forceinline__ void tile_steps_pair(
         // ---- coherence vector and polarisation at every point
         if (qm) {
 #pragma unroll
-            for (int q = 0; q < HP; q++) cvr2_update_pair(u[q], ul[q], e[q], pt[q], cf);
+            for (int q = 0; q < HP; q++) cvr2_update_pair<SP>(u[q], ul[q], e[q], pt[q], cf);
         }
         if (!interior) {
 #pragma unroll

@@ -578,7 +578,11 @@ __device__ __forceinline__ void step_body(const kparams<T>& p, uint32_t tile, ui
     if (uniform) {
         if constexpr (pair_path<T, ALGO, LEV, C, TC>()) {
             // two points per instruction (pair_steps.cuh)
-            tile_steps_pair<C, NT>(p, td, rd, l0, nsteps, step0, E, H, P, R, Rl, M, sh_coef, tl, sh_a, sh_b);
+            if (cvr2_sparse(sh_coef))
+                tile_steps_pair<C, NT, true>(p, td, rd, l0, nsteps, step0, E, H, P, R, Rl, M, sh_coef, tl, sh_a, sh_b);
+            else
+                tile_steps_pair<C, NT, false>(p, td, rd, l0, nsteps, step0, E, H, P, R, Rl, M, sh_coef, tl, sh_a,
+                                              sh_b);
         } else {
             const bool ok = tile_steps<T, ALGO, LEV, C, NT, true, TC>(p, td, rd, l0, nsteps, step0, E, El, H, Hl,
                                                                       P, R, Rl, M, sh_coef, tl, sh_a, sh_al,

@@ -59,6 +59,10 @@ def test_gpu_matches_golden(native, case, prec):
      dict(num_gridpoints=2000, num_timesteps=500)),
     ("gpu-fdtd-2lvl-cvr-rodr-fp32", "ziolkowski1995",
      dict(num_gridpoints=2500, endtime=40e-15)),
+    # off-diagonal Hamiltonian and complex dipole: a dense 2-level block
+    # (the pair path's general variant)
+    ("gpu-fdtd-2lvl-cvr-rodr-fp32", "random_nlvl",
+     dict(N=2, num_gridpoints=3000, num_timesteps=700, seed=2, e_seed=3e7)),
 ])
 def test_tuning_does_not_change_results(native, name, setup, kw):
     """Temporal blocking depth and tile shape change only the schedule:
