@@ -77,7 +77,7 @@ struct kparams {
 // ------------------------------------------------------------ helpers
 
 // sin(x) and 1 - cos(x). For small |x| by their Taylor series (enough
-// terms for the type's precision: truncation below 1e-12 relative in
+// terms for the type's precision: truncation below 1e-10 relative in
 // float, 1e-30 in double); beyond that by the library sincos.
 template<typename T>
 __device__ __forceinline__ void rot_coeffs(T x, T& s, T& s2);
@@ -85,10 +85,17 @@ __device__ __forceinline__ void rot_coeffs(T x, T& s, T& s2);
 template<>
 __device__ __forceinline__ void rot_coeffs<float>(float x, float& s, float& s2)
 {
-    // |x| < 1/16 (the field rotation per step is far smaller in every
-    // workload here: ~1e-3): the series to x^7 and x^8, Horner in x^2;
-    // the first omitted terms are below 1e-14 of the result
-    if (fabsf(x) < 0.0625f) {
+    // |x| < 1/128 (the field rotation per step in the workloads here is
+    // ~1e-3): sin x = x - x^3/6, 1 - cos x = x^2/2 - x^4/24; the first
+    // omitted terms (x^4/120 and x^4/360 of the result) are below 4e-11 of
+    // it, over 1000 times below half an FP32 ulp
+    if (fabsf(x) < 0.0078125f) {
+        const float x2 = x * x;
+        s = fmaf(x * x2, -1.0f / 6.0f, x);
+        s2 = x2 * fmaf(x2, -1.0f / 24.0f, 0.5f);
+    } else if (fabsf(x) < 0.0625f) {
+        // |x| < 1/16: the series to x^7 and x^8, Horner in x^2; the first
+        // omitted terms are below 1e-14 of the result
         const float x2 = x * x;
         // sin x = x (1 - x^2/3! + x^4/5! - x^6/7!)
         float t = fmaf(x2, -1.0f / 5040.0f, 1.0f / 120.0f);
@@ -440,7 +447,7 @@ __device__ __forceinline__ void cvr_update_df(float (&uh)[V], float (&ul)[V], fl
         constexpr int k = decltype(K)::value;
         float sn, s2;
         rot_coeffs<float>(c.th(k) * e, sn, s2);
-        const float a = uh[2 * k], b = uh[2 * k + 1];
+        const float a = r[2 * k], b = r[2 * k + 1];
         d[2 * k] = -fmaf(s2, a, sn * b);
         d[2 * k + 1] = fmaf(sn, a, -s2 * b);
         r[2 * k] = a + d[2 * k];

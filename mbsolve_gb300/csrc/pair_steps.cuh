@@ -101,7 +101,11 @@ __device__ __forceinline__ void cvr2_update_pair(float2 (&uh)[3], float2 (&ul)[3
     const float2 z = bc(0.0f);
     const float2 x = mul(c.th, e);
     float2 sn, s2;
-    if (fabsf(x.x) < 0.0625f && fabsf(x.y) < 0.0625f) {
+    if (fabsf(x.x) < 0.0078125f && fabsf(x.y) < 0.0078125f) {
+        const float2 x2 = mul(x, x);
+        sn = fma(mul(x, x2), bc(-1.0f / 6.0f), x);
+        s2 = mul(x2, fma(x2, bc(-1.0f / 24.0f), bc(0.5f)));
+    } else if (fabsf(x.x) < 0.0625f && fabsf(x.y) < 0.0625f) {
         const float2 x2 = mul(x, x);
         float2 t = fma(x2, bc(-1.0f / 5040.0f), bc(1.0f / 120.0f));
         t = fma(x2, t, bc(-1.0f / 6.0f));
