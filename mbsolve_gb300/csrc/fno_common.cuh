@@ -200,9 +200,21 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
     return *reinterpret_cast<const uint32_t*>(&v);
 }
 
+// GELU(x) = 0.5 x (1 + erf(x / sqrt 2)) with erf by Abramowitz and Stegun,
+// Handbook of Mathematical Functions (1964), 7.1.26 (|error| <= 1.5e-7):
+// erfc z = t (a1 + t (a2 + t (a3 + t (a4 + t a5)))) exp(-z^2),
+// t = 1 / (1 + p z), z = |x| / sqrt 2. Branch-free; x < 0 takes
+// 0.5 x erfc z directly (no cancellation), x >= 0 takes x - 0.5 x erfc z.
 __device__ __forceinline__ float gelu(float x)
 {
-    return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f));
+    const float z = fabsf(x) * 0.70710678118654752f;
+    const float t = __fdividef(1.0f, fmaf(0.3275911f, z, 1.0f));
+    float q = fmaf(t, 1.061405429f, -1.453152027f);
+    q = fmaf(t, q, 1.421413741f);
+    q = fmaf(t, q, -0.284496736f);
+    q = fmaf(t, q, 0.254829592f);
+    const float h = 0.5f * x * (t * q * __expf(-z * z));
+    return x < 0.0f ? h : x - h;
 }
 
 __device__ __forceinline__ float gelu_grad(float x)

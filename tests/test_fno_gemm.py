@@ -86,6 +86,25 @@ def test_segments_negate_accum_bias_gelu(K):
     _cmp(c, gel, tol=1e-2)   # BF16 output
 
 
+def test_gelu_epilogue_fp32(K):
+    """The epilogues' GELU (erf by Abramowitz and Stegun 7.1.26, |error| <=
+    1.5e-7) against the exact erf GELU in float64, stored in FP32: zero
+    operands, so C(0, j) = GELU(bias[j]) over inputs from -12 to 12."""
+    from mbsolve_gb300 import capi_types as T
+    n = 8192
+    x = torch.linspace(-12.0, 12.0, n, dtype=torch.float32)
+    c = torch.zeros(1, n, device="cuda")
+    K.gemm(1, n, [K.Seg(torch.zeros(1, 1).cuda(), 0, 1, 0, 0,
+                        torch.zeros(n, 1).cuda(), 0, 1, 0, 0, 1)], c, 0, n, 1,
+           act=T.MBG_ACT_GELU, bias=x.cuda())
+    torch.cuda.synchronize()
+    xd = x.double()
+    want = 0.5 * xd * (1.0 + torch.erf(xd / np.sqrt(2.0)))
+    err = (c.cpu().double()[0] - want).abs()
+    # 0.5 |x| 1.5e-7 from the erf formula, a few FP32 roundings
+    assert (err <= 4e-7 * xd.abs().clamp_min(1.0)).all(), float(err.max())
+
+
 def test_gelu_backward_epilogue(K):
     from mbsolve_gb300 import capi_types as T
     g = torch.Generator().manual_seed(3)
