@@ -264,19 +264,24 @@ def _mixed_3lvl():
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
 def test_mixed_ensemble_equals_single_runs(native, algo, prec):
     """Runs of every shape in one launch sequence give exactly the single
-    runs' results (and, in FP64, the oracle's)."""
+    runs' results (and, in FP64, the oracle's). Both sides run the same
+    tuning: FP32 Cayley renormalises the trace once per launch, so its
+    results follow the launch depth wherever the trace has drifted (the
+    autotuner may pick different depths for the ensemble and a single
+    run)."""
     from mbsolve_gb300 import ensemble
     name = "gpu-fdtd-3lvl-%s-%s" % (algo, prec)
     specs = _mixed_3lvl()
+    t = helpers.tuning(1, 128, 8, 2)
     mb.material.clear_library()
     pairs = [helpers.build_setup({"setup": s, "kw": kw}) for s, kw in specs]
-    ens = ensemble.ensemble(name, pairs)
+    ens = ensemble.ensemble(name, pairs, t)
     ens.run()
     assert ens.status() == 0
     for i, (s, kw) in enumerate(specs):
         mb.material.clear_library()
         dev, sce = helpers.build_setup({"setup": s, "kw": kw})
-        _, single = helpers.gpu_results(name, dev, sce)
+        _, single = helpers.gpu_results(name, dev, sce, t)
         got = [r.as_array() for r in ens.results(i)]
         for a, b in zip(got, single):
             assert np.array_equal(a, b), (s, i)
