@@ -78,3 +78,38 @@ def test_bf16_mode_stays_close_to_float64():
     l16, g16, _ = O.forward_backward(sh, theta, X, t, bf16=True)
     assert abs(l16 - l64) < 2e-2 * l64
     assert np.linalg.norm(g16 - g64) < 5e-2 * np.linalg.norm(g64)
+
+
+def test_gelu_erf_formula_in_the_kernel_source():
+    """The kernels' GELU evaluates erf by Abramowitz and Stegun 7.1.26; the
+    constants as written in the CUDA source, evaluated in float64, keep
+    |erf error| <= 1.5e-7 (the published bound) and the GELU error
+    <= 0.5 |x| 1.5e-7 over -8..8 (the FP32 evaluation is checked on the
+    GPU in tests/test_fno_gemm.py)."""
+    import os
+    import re
+    path = os.path.join(os.path.dirname(__file__), "..", "mbsolve_gb300",
+                        "csrc", "fno_common.cuh")
+    src = open(path).read()
+    body = src[src.index("float gelu(float x)"):]
+    body = body[:body.index("\n}\n")]
+    num = r"(-?\d+\.\d+)f"
+    p = float(re.search(r"fmaf\(" + num + r", z, 1\.0f\)", body).group(1))
+    first = re.search(r"fmaf\(t, " + num + r", " + num + r"\)", body)
+    rest = [float(v) for v in re.findall(r"fmaf\(t, q, " + num + r"\)", body)]
+    a = [rest[2], rest[1], rest[0], float(first.group(2)),
+         float(first.group(1))]  # a1 .. a5
+    assert p == 0.3275911 and len(rest) == 3
+    z = np.linspace(0.0, 8.0 / math.sqrt(2.0), 20001)
+    t = 1.0 / (1.0 + p * z)
+    erfc = t * (a[0] + t * (a[1] + t * (a[2] + t * (a[3] + t * a[4])))) * \
+        np.exp(-z * z)
+    exact = np.array([math.erfc(v) for v in z])
+    assert np.abs(erfc - exact).max() <= 1.5e-7
+    x = z * math.sqrt(2.0)
+    for s in (1.0, -1.0):
+        xs = s * x
+        got = np.where(xs < 0, 0.5 * xs * erfc, xs - 0.5 * xs * erfc)
+        want = 0.5 * xs * (1.0 + np.array([math.erf(v / math.sqrt(2.0))
+                                           for v in xs]))
+        assert (np.abs(got - want) <= 0.5 * np.abs(xs) * 1.5e-7 + 1e-15).all()
