@@ -448,18 +448,22 @@ __global__ void __launch_bounds__(LNTH, 1) spectral_layer_kernel(const layer_par
         auto project = [&](int w) {
             wait_bar_warp(bar(B_FH + (w & 1)), (w >> 1) & 1, abort, lane);
             fence_after();
-            float ysum = 0.0f;
+            // two partial sums (even and odd columns), packed FP32 pairs
+            float2 ys = make_float2(0.0f, 0.0f);
 #pragma unroll
             for (int q = 0; q < 2; q++) {
                 float h[16];
                 tmem_ld16(tmem + tlane + 256u + (uint32_t) ((w & 1) * 128 + qt * 32 + q * 16), h);
 #pragma unroll
-                for (int k = 0; k < 16; k++) {
+                for (int k = 0; k < 16; k += 2) {
                     const int j = qt * 32 + q * 16 + k;
-                    const float z = bf16r(gelu(h[k] + small[SM_BQ1 + j]));
-                    ysum = fmaf(z, small[SM_Q2 + j], ysum);
+                    const float2 v = __fadd2_rn(make_float2(h[k], h[k + 1]),
+                                                *reinterpret_cast<const float2*>(small + SM_BQ1 + j));
+                    const float2 z = __bfloat1622float2(__float22bfloat162_rn(gelu2(v)));
+                    ys = __ffma2_rn(z, *reinterpret_cast<const float2*>(small + SM_Q2 + j), ys);
                 }
             }
+            const float ysum = ys.x + ys.y;
             fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(bar(B_EH + (w & 1)));
@@ -513,13 +517,10 @@ __global__ void __launch_bounds__(LNTH, 1) spectral_layer_kernel(const layer_par
             uint32_t pk[8];
 #pragma unroll
             for (int j = 0; j < 16; j += 2) {
-                float v0 = x[j] + small[SM_BIAS + qt * 16 + j];
-                float v1 = x[j + 1] + small[SM_BIAS + qt * 16 + j + 1];
-                if (GELU) {
-                    v0 = gelu(v0);
-                    v1 = gelu(v1);
-                }
-                pk[j >> 1] = pack_bf16(v0, v1);
+                float2 v = __fadd2_rn(make_float2(x[j], x[j + 1]),
+                                      *reinterpret_cast<const float2*>(small + SM_BIAS + qt * 16 + j));
+                if (GELU) v = gelu2(v);
+                pk[j >> 1] = pack_bf16(v.x, v.y);
             }
             if (!last) {
                 // the output image (free once the bulk store of tile u-1 has read it)
