@@ -12,6 +12,7 @@
 
 #include "../../include/mbsolve_fno.h"
 #include "../../include/mbsolve_gb300.h"
+#include "f32x2.cuh"
 
 namespace mbg {
 void set_last_error(const char* msg);
@@ -218,36 +219,22 @@ __device__ __forceinline__ float gelu(float x)
 }
 
 // gelu() on two values: lane by lane the same operations, the multiplies
-// and fused multiply-adds as packed FP32 pairs (fma/mul/sub.rn.f32x2), the
-// reciprocal and the exponential per lane
-__device__ __forceinline__ float2 pair_bc(float v) { return make_float2(v, v); }
-
-__device__ __forceinline__ float2 pair_sub(float2 a, float2 b)
-{
-    float2 r;
-    asm("{.reg .b64 pa, pb, pd;\n\t"
-        "mov.b64 pa, {%2, %3};\n\t"
-        "mov.b64 pb, {%4, %5};\n\t"
-        "sub.rn.f32x2 pd, pa, pb;\n\t"
-        "mov.b64 {%0, %1}, pd;}"
-        : "=f"(r.x), "=f"(r.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return r;
-}
-
+// and fused multiply-adds as packed FP32 pairs (f32x2.cuh), the reciprocal
+// and the exponential per lane
 __device__ __forceinline__ float2 gelu2(float2 x)
 {
-    const float2 z = __fmul2_rn(make_float2(fabsf(x.x), fabsf(x.y)), pair_bc(0.70710678118654752f));
-    const float2 d = __ffma2_rn(pair_bc(0.3275911f), z, pair_bc(1.0f));
+    using namespace f2;
+    const float2 z = mul(make_float2(fabsf(x.x), fabsf(x.y)), bc(0.70710678118654752f));
+    const float2 d = fma(bc(0.3275911f), z, bc(1.0f));
     const float2 t = make_float2(__fdividef(1.0f, d.x), __fdividef(1.0f, d.y));
-    float2 q = __ffma2_rn(t, pair_bc(1.061405429f), pair_bc(-1.453152027f));
-    q = __ffma2_rn(t, q, pair_bc(1.421413741f));
-    q = __ffma2_rn(t, q, pair_bc(-0.284496736f));
-    q = __ffma2_rn(t, q, pair_bc(0.254829592f));
-    const float2 zz = __fmul2_rn(z, z);
+    float2 q = fma(t, bc(1.061405429f), bc(-1.453152027f));
+    q = fma(t, q, bc(1.421413741f));
+    q = fma(t, q, bc(-0.284496736f));
+    q = fma(t, q, bc(0.254829592f));
+    const float2 zz = mul(z, z);
     const float2 e = make_float2(__expf(-zz.x), __expf(-zz.y));
-    const float2 h = __fmul2_rn(__fmul2_rn(pair_bc(0.5f), x), __fmul2_rn(__fmul2_rn(t, q), e));
-    const float2 xh = pair_sub(x, h);
+    const float2 h = mul(mul(bc(0.5f), x), mul(mul(t, q), e));
+    const float2 xh = sub(x, h);
     return make_float2(x.x < 0.0f ? h.x : xh.x, x.y < 0.0f ? h.y : xh.y);
 }
 
