@@ -268,3 +268,41 @@ def test_cayley_block_structure_flag(native, setup, kw):
         assert np.all(B0[~mask] == 0.0)
     else:
         assert np.any(B0[~mask] != 0.0)
+
+
+def _cvr2_zeros(block, L):
+    """The entries that the 2-level pair kernel's sparse variant skips
+    (cvr2_sparse in pair_steps.cuh), as FP32 values."""
+    V = L["V"]
+    Bd = block[L["Bd"]:L["Bd"] + V * V].reshape(V, V).astype(np.float32)
+    Bdl = block[L["Bdl"]:L["Bdl"] + V * V].reshape(V, V).astype(np.float32)
+    g = block[L["g"]:L["g"] + V].astype(np.float32)
+    idx = [(0, 1), (1, 0), (1, 2), (2, 1)]
+    return [Bd[i] for i in idx] + [Bdl[i] for i in idx] + [g[1]]
+
+
+def test_two_level_presets_take_the_sparse_pair_update(native):
+    """The benchmark's 2-level media (diagonal Hamiltonian, real dipole)
+    give blocks with the exact zeros that let the pair kernel skip 10
+    products per pair; a random 2-level medium (off-diagonal Hamiltonian,
+    complex dipole) has none of them, so the GPU tests that use it run the
+    general variant."""
+    from mbsolve_gb300 import _native
+    L = _native.material_layout("cvr-rodr", 2)
+    runs, _ = setups.ensemble_2lvl(num_runs=8, num_timesteps=100, seed=0)
+    runs.append(setups.sit_2lvl(num_gridpoints=64, num_timesteps=10))
+    runs.append(setups.ziolkowski1995(num_gridpoints=256, endtime=1e-15))
+    for dev, sce in runs:
+        b = mb.to_pod(dev, sce)
+        for i in range(b.device.num_materials):
+            mat = b.device.materials[i]
+            if not mat.qm:
+                continue
+            blk = _constants(native, "cvr-rodr", mat, 1.5e-17)
+            assert all(v == 0.0 for v in _cvr2_zeros(blk, L))
+    mb.material.clear_library()
+    dev, sce = setups.random_nlvl(N=2, num_gridpoints=64, num_timesteps=10,
+                                  seed=2)
+    b = mb.to_pod(dev, sce)
+    blk = _constants(native, "cvr-rodr", b.device.materials[0], 1.5e-17)
+    assert all(v != 0.0 for v in _cvr2_zeros(blk, L))
