@@ -15,9 +15,11 @@
 // Neighbour values cross thread boundaries by warp shuffles and cross warp
 // boundaries through shared memory (two barriers per step). Garbage from
 // the tile edges moves one point per step, so after `nsub <= halo` steps
-// the output range is exact. Points outside the run keep zero state and
-// are never updated; the reference's index rules (no H update at i = 0,
-// H[N] = 0) give them no influence on the run.
+// the output range is exact. Points outside the run keep zero state (the
+// one-point loop never updates them; the packed-pair loop of uniform
+// 2-level FP32 tiles, pair_steps.cuh, updates them with their neighbours
+// and puts them back after each step); the reference's index rules (no H
+// update at i = 0, H[N] = 0) give them no influence on the run.
 //
 // FP32 kernels keep the density state, and E and H in all but the 2-level
 // kernel, as unevaluated sums hi + lo of two floats updated with
@@ -27,7 +29,9 @@
 // the float pairs the FP32 result tracks the FP64 one to ~1e-7 while
 // polarisation and all matrix work stay in FP32. The 2-level kernel keeps
 // E and H in plain FP32 (one rounding per update by fma): ~6e-6 over 1e5
-// steps, within the 1e-5 target, for 22 % more throughput.
+// steps, within the 1e-5 target, for 22 % more throughput; on uniform
+// tiles it updates two points per instruction (packed FP32 pairs, the
+// same roundings).
 #pragma once
 
 #include <cuda_runtime.h>
