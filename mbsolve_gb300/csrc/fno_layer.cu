@@ -86,6 +86,9 @@ constexpr int OFF_SMALL = OFF_W + B_IMG;
 constexpr int SM_BIAS = 0, SM_BQ1 = 64, SM_Q2 = 192, SM_RED = 320;  // floats
 constexpr int SMALL_FLOATS = SM_RED + 2 * 4 * 128;
 constexpr int LAYER_SMEM = OFF_SMALL + SMALL_FLOATS * 4 + 128;  // + alignment slack
+// the epilogues read bias, bq1 and q2 as float2 pairs at even columns
+static_assert(OFF_SMALL % 8 == 0 && SM_BIAS % 2 == 0 && SM_BQ1 % 2 == 0 && SM_Q2 % 2 == 0,
+              "small parameters: 8-byte aligned pairs");
 // the last basis slot's unread M rows (32 KB from its start) stay inside the map
 static_assert(OFF_F + (NFR - 1) * F_IMG + 2 * F_IMG <= OFF_OUT, "basis slot overrun");
 static_assert(NX * X_SLOT + NXI * XI_IMG <= NGV * GV_SLOT && IMG <= NFR * F_IMG && IMG <= VT_IMG, "aliases");
